@@ -1,0 +1,124 @@
+"""Write the golden fixtures in this folder from the reference's own compiled
+sources (oracle/_ref/libpcd_ref.so, built by oracle/Makefile from the mounted
+reference tree).  Run from the repository root:
+
+    python tests/golden/make_golden.py
+
+Fixtures (all float64, seeded inputs, the reference run with max_threads=1):
+
+* solver_cases.npz  -- poisson_solver (solver.cpp:70-148) on small grids:
+  zero and warm starts, ragged sizes, a NaN hole, an iteration cap.
+* utils_cases.npz   -- calculate_gradient / calculate_divergence /
+  subtractAverage / scale_matrix_proportional / bilinearInterpolation.
+* pipeline_r{16,32,64}.npz -- Caustic_design replay of main.cpp:216-262 at
+  mesh resolution r (grid 4r): per-iteration step sizes, target areas, the
+  first iteration's errors/raster, final phi / target points, and after the
+  three height iterations h and the source points.
+"""
+from __future__ import annotations
+
+import os
+import sys
+
+import numpy as np
+
+ROOT = os.path.abspath(os.path.join(os.path.dirname(__file__), "..", ".."))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+import oracle as O  # noqa: E402
+from poisson_caustic_design_gb300 import inputs  # noqa: E402
+
+OUT = os.path.dirname(os.path.abspath(__file__))
+
+
+def solver_cases(R: O.Ref):
+    cases = {}
+    rng = np.random.default_rng(20241203)
+
+    def add(name, b, phi0, max_iter, tol):
+        phi = phi0.copy()
+        R.poisson_solver(b, phi, max_iter, tol, 1)
+        cases[f"{name}/b"] = b
+        cases[f"{name}/phi0"] = phi0
+        cases[f"{name}/phi"] = phi
+        cases[f"{name}/params"] = np.array([max_iter, tol])
+
+    b = rng.standard_normal((5, 7)); b -= b.mean()
+    add("rand_7x5", b, np.zeros_like(b), 100000, 1e-9)
+    b = rng.standard_normal((17, 33)); b -= b.mean()
+    add("warm_33x17", b, rng.standard_normal((17, 33)), 100000, 1e-7)
+    add("gauss_64", inputs.poisson_rhs(64, 1, "gaussian"), np.zeros((64, 64)), 100000, 1e-7)
+    add("binary_96x80", inputs.poisson_rhs(96, 2, "binary", m=80), np.zeros((80, 96)), 100000, 1e-7)
+    add("gauss_128", inputs.poisson_rhs(128, 3, "gaussian"), np.zeros((128, 128)), 100000, 1e-7)
+    b = inputs.poisson_rhs(48, 4, "gaussian", m=40)
+    b[10:14, 20:27] = np.nan
+    b[0, 0] = np.nan
+    add("nanhole_48x40", b, np.zeros_like(b), 100000, 1e-8)
+    add("capped_64", inputs.poisson_rhs(64, 5, "binary"), np.zeros((64, 64)), 50, 1e-12)
+    add("single_row_16x1", rng.standard_normal((1, 16)) - 0.0, np.zeros((1, 16)), 300, 1e-9)
+    np.savez_compressed(os.path.join(OUT, "solver_cases.npz"), **cases)
+
+
+def utils_cases(R: O.Ref):
+    rng = np.random.default_rng(7)
+    g = rng.standard_normal((19, 23))
+    g2 = rng.standard_normal((19, 23))
+    gx, gy = R.gradient(g)
+    pts = np.array([[-0.5, -0.5], [3.25, 2.75], [22.5, 18.5], [0.0, 0.0], [21.999, 17.2], [10.0, 5.5]])
+    gn = g.copy(); gn[3, 4] = np.nan
+    np.savez_compressed(
+        os.path.join(OUT, "utils_cases.npz"),
+        g=g, g2=g2, gx=gx, gy=gy, div=R.divergence(g, g2), sub=R.subtract_average(gn), gn=gn,
+        scaled=R.scale_proportional(g * 3.0 + 1.0, 0.0, 1.0), pts=pts,
+        bil=np.array([R.bilinear(g, x, y) for x, y in pts]),
+    )
+
+
+def pipeline(R: O.Ref, res: int, seed: int, width=0.5, focal=1.5, thickness=0.1, conv=0.01):
+    img = inputs.pipeline_image(res, seed)
+    d = O.RefDesign(R, res, res, 4 * res, 4 * res, width, width, focal, thickness, 1)
+    d.initialize(img)
+    out = {"image": img, "params": np.array([res, width, focal, thickness, conv, seed]),
+           "target_areas": d.get("target_areas")}
+    steps = []
+    for itr in range(50):
+        s = d.transport_iteration()
+        steps.append(s)
+        if itr == 0:
+            out["errors_0"] = d.get("errors")
+            out["raster_0"] = d.get("raster")
+            out["phi_0"] = d.get("phi")
+            out["target_points_0"] = d.get("target_points")
+        if s < conv:
+            break
+    out["steps"] = np.array(steps)
+    out["phi"] = d.get("phi")
+    out["target_points"] = d.get("target_points")
+    for itr in range(3):
+        d.height_iteration(itr)
+        if itr == 0:
+            out["normals_x_0"] = d.get("normals_x")
+            out["normals_y_0"] = d.get("normals_y")
+            out["divergence_0"] = d.get("divergence")
+            out["h_0"] = d.get("h")
+            out["source_points_0"] = d.get("source_points")
+    out["h"] = d.get("h")
+    out["source_points"] = d.get("source_points")
+    d.close()
+    np.savez_compressed(os.path.join(OUT, f"pipeline_r{res}.npz"), **out)
+    return len(steps)
+
+
+def main():
+    O.build(ref=True)
+    R = O.Ref()
+    solver_cases(R)
+    utils_cases(R)
+    for res, seed in ((16, 3), (32, 11), (64, 29)):
+        n = pipeline(R, res, seed)
+        print(f"pipeline r{res}: {n} transport iterations")
+
+
+if __name__ == "__main__":
+    main()
