@@ -1,0 +1,182 @@
+/*
+ * pcd.h -- C ABI of the GB300 (sm_103a) Poisson caustic-design library
+ * (libpcd_gb300.so).
+ *
+ * Plain C types only: pointers, sizes, enums and small POD structs.  Every
+ * entry point returns a pcd_status; none exits the process or falls back to a
+ * CPU path.  Grids are row-major doubles g[y*ld + x] (the reference's
+ * vector<vector<double>> g[y][x]); mesh points are n x 3 doubles (x, y, z).
+ *
+ * The interfaces replaced, by reference file:line (dylanmsu/poisson_caustic_design):
+ *   pcd_poisson_solver           <- poisson_solver()            src/solver.h:8, src/solver.cpp:70-148
+ *   pcd_poisson_solve(_device)   <- same, with explicit options/statistics (new surface)
+ *   pcd_subtract_average_device  <- subtractAverage()           src/utils.h:13, src/utils.cpp:60-86
+ *   pcd_gradient_device          <- calculate_gradient()        src/utils.h:18, src/utils.cpp:3-20
+ *   pcd_divergence_device        <- calculate_divergence()      src/utils.h:19, src/utils.cpp:22-39
+ *   pcd_design_*                 <- class Caustic_design        src/caustic_design.h:7-66
+ *       pcd_design_create            set_mesh_resolution / set_domain_resolution /
+ *                                    set_mesh_size / set_lens_focal_length /
+ *                                    set_lens_thickness     caustic_design.h:53-58
+ *       pcd_design_initialize        initialize_solvers()   caustic_design.cpp:334-364
+ *       pcd_design_transport_iteration perform_transport_iteration() caustic_design.cpp:190-266
+ *       pcd_design_height_iteration  perform_height_map_iteration() caustic_design.cpp:269-332
+ *       pcd_design_get_grid / _get_vertices  the public members phi, h, raster,
+ *                                    divergence, norm_x, norm_y, errors, target_areas,
+ *                                    mesh->target_points / source_points (caustic_design.h:16-30,
+ *                                    mesh.h:51-52)
+ */
+#ifndef PCD_H
+#define PCD_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    PCD_OK = 0,
+    PCD_NOT_CONVERGED = 1,   /* stopped at max_iterations (the reference stops silently) */
+    PCD_BAD_ARG = 2,
+    PCD_DEVICE_ERROR = 3,    /* a CUDA call failed; pcd_last_error() has the text */
+    PCD_TIMEOUT = 4,         /* a bounded device-side wait gave up */
+    PCD_RASTER_MISS = 5,     /* a grid sample fell in no triangle (the reference calls exit(0)) */
+    PCD_NO_DEVICE = 6,
+    PCD_FALLBACK_USED = 7    /* learned warm start rejected; solved from a zero guess */
+} pcd_status;
+
+typedef enum {
+    /* max |delta| of one sweep below tol: the reference's test (solver.cpp:142) */
+    PCD_STOP_MAX_UPDATE = 0,
+    /* ||b - L phi||_2 / ||b||_2 <= tol, evaluated in FP64 */
+    PCD_STOP_REL_RESIDUAL = 1
+} pcd_stop;
+
+typedef enum {
+    PCD_PREC_FP64 = 0,       /* FP64 red-black SOR sweeps */
+    PCD_PREC_MIXED = 1       /* FP32 sweeps on the error equation, FP64 residual/update */
+} pcd_precision;
+
+typedef struct {
+    int max_iterations;      /* sweep cap (reference callers pass 100000) */
+    double tol;              /* threshold of `stop` */
+    int stop;                /* pcd_stop */
+    int precision;           /* pcd_precision */
+    double omega;            /* relaxation factor: > 0 as given; 0 the reference's 2/(1+pi/width)
+                                (solver.cpp:71); < 0 the optimum for the Neumann operator,
+                                2/(1+sin t) with cos t = (1+cos(pi/max(width,height)))/2 */
+    int check_every;         /* sweeps between stop tests; 0 = auto.  The launch schedule tests
+                                max |delta| after every sweep; the persistent one every
+                                check_every sweeps (default 8 FP64 / 16 mixed), so it may run
+                                up to check_every-1 sweeps past the first passing sweep */
+    int refine_every;        /* FP32 sweeps between FP64 residual replacements (mixed); 0 = auto */
+    int warm_start;          /* 1: phi holds the initial guess (reference behaviour); 0: start at 0 */
+    int schedule;            /* pcd_schedule */
+} pcd_solve_opts;
+
+typedef enum {
+    PCD_SCHED_AUTO = 0,        /* cluster, else persistent, else launches, as the grid allows */
+    PCD_SCHED_LAUNCHES = 1,    /* one kernel per half sweep, CUDA-graph chunks (any grid) */
+    PCD_SCHED_PERSISTENT = 2,  /* one cooperative launch per solve, bands in shared memory
+                                  (no NaN cells, band fits on chip) */
+    PCD_SCHED_CLUSTER = 3      /* mixed precision with the relative-residual stop: FP32 sweeps
+                                  on one 16-CTA cluster (grid fits in its shared memory),
+                                  FP64 defect correction on all SMs between cycles */
+} pcd_schedule;
+
+typedef struct {
+    int sweeps;              /* full red+black sweeps run */
+    int converged;           /* 1 if the stop test passed */
+    double rel_residual;     /* ||b - L phi|| / ||b|| at exit (FP64, non-NaN cells) */
+    double max_residual;     /* max |b - L phi| at exit */
+    double last_max_update;  /* max |delta| of the last sweep (when tracked) */
+    double device_ms;        /* device time of the solve (CUDA events) */
+    int residual_checks;     /* FP64 residual evaluations */
+    double sweep_ms;         /* device time of the sweep kernel(s) alone (CUDA events) */
+    int schedule_used;       /* pcd_schedule that ran (1 launches, 2 persistent) */
+} pcd_solve_stats;
+
+typedef struct pcd_ctx pcd_ctx;
+typedef struct pcd_design pcd_design;
+
+/* ---- context ---------------------------------------------------------- */
+int pcd_ctx_create(int device, pcd_ctx **out);
+int pcd_ctx_destroy(pcd_ctx *ctx);
+/* Stream the context launches on (a cudaStream_t). */
+void *pcd_ctx_stream(pcd_ctx *ctx);
+const char *pcd_last_error(void);
+const char *pcd_status_string(int status);
+int pcd_solve_opts_default(pcd_solve_opts *opts);
+/* Number of kernels this library launched in this process (monotonic). */
+unsigned long long pcd_kernel_launches(void);
+
+/* ---- Poisson solve ------------------------------------------------------ */
+/* Drop-in for poisson_solver(D, phi, width, height, max_iterations,
+ * convergence_threshold, max_threads), solver.cpp:70: solves
+ * sum_nbr phi - cnt*phi = D in place on phi (host arrays, width*height,
+ * row-major), phi is the warm start, stops when one sweep's max |delta| falls
+ * below convergence_threshold or after max_iterations sweeps.  Neighbours
+ * outside the grid or whose D is NaN are excluded (Neumann).  max_threads is
+ * accepted and ignored.  Uses a process-wide context on the current device. */
+int pcd_poisson_solver(const double *D, double *phi, int width, int height, int max_iterations,
+                       double convergence_threshold, int max_threads);
+
+/* Host arrays, explicit options and statistics. */
+int pcd_poisson_solve(pcd_ctx *ctx, const double *b, double *phi, int width, int height,
+                      const pcd_solve_opts *opts, pcd_solve_stats *stats);
+
+/* Device arrays with leading dimension ld (elements, >= width) on `stream`
+ * (NULL = the context's stream).  b is read, phi updated in place. */
+int pcd_poisson_solve_device(pcd_ctx *ctx, const double *b, double *phi, int width, int height,
+                             int ld, const pcd_solve_opts *opts, pcd_solve_stats *stats,
+                             void *stream);
+
+/* ---- grid utilities on device arrays (dense, ld == width) -------------- */
+int pcd_subtract_average_device(pcd_ctx *ctx, double *g, int width, int height, void *stream);
+int pcd_gradient_device(pcd_ctx *ctx, const double *g, double *gx, double *gy, int width,
+                        int height, void *stream);
+int pcd_divergence_device(pcd_ctx *ctx, const double *nx, const double *ny, double *div,
+                          int width, int height, void *stream);
+
+/* ---- Caustic_design ----------------------------------------------------- */
+typedef enum {
+    PCD_GRID_PHI = 0, PCD_GRID_H = 1, PCD_GRID_RASTER = 2, PCD_GRID_DIVERGENCE = 3,
+    PCD_GRID_NORM_X = 4, PCD_GRID_NORM_Y = 5
+} pcd_grid;
+
+typedef enum {
+    PCD_VERT_TARGET_POINTS = 10, PCD_VERT_SOURCE_POINTS = 11, PCD_VERT_TARGET_AREAS = 12,
+    PCD_VERT_ERRORS = 13, PCD_VERT_NORMALS_X = 14, PCD_VERT_NORMALS_Y = 15,
+    PCD_VERT_GRADIENT_X = 16, PCD_VERT_GRADIENT_Y = 17
+} pcd_vertex_field;
+
+typedef struct {
+    int mesh_res_x, mesh_res_y;  /* set_mesh_resolution */
+    int res_x, res_y;            /* set_domain_resolution (Poisson grid) */
+    double width, height;        /* set_mesh_size */
+    double focal_l;              /* set_lens_focal_length */
+    double thickness;            /* set_lens_thickness */
+    pcd_solve_opts transport;    /* solve options of the transport iterations */
+    pcd_solve_opts height_solve; /* solve options of the height iterations */
+} pcd_design_params;
+
+/* Defaults: the reference's solves (max |delta| < 1e-7 transport,
+ * < 1e-8 height, 100000 sweeps, FP64). */
+int pcd_design_params_default(pcd_design_params *p);
+int pcd_design_create(pcd_ctx *ctx, const pcd_design_params *p, pcd_design **out);
+int pcd_design_destroy(pcd_design *d);
+/* image: res_y x res_x gray grid (host), as passed to initialize_solvers. */
+int pcd_design_initialize(pcd_design *d, const double *image);
+/* *step_out = max vertex displacement / width (caustic_design.cpp:253-265). */
+int pcd_design_transport_iteration(pcd_design *d, double *step_out, pcd_solve_stats *stats);
+/* *update_out = sum of squared height changes (mesh.cpp:735-741). */
+int pcd_design_height_iteration(pcd_design *d, int itr, double *update_out, pcd_solve_stats *stats);
+/* Copy a grid (res_y x res_x) or vertex field (n or n x 3) to host memory. */
+int pcd_design_get_grid(pcd_design *d, int which, double *host_out);
+int pcd_design_get_vertices(pcd_design *d, int which, double *host_out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PCD_H */

@@ -57,6 +57,9 @@ class Port:
         self.L = L
         L.pcdo_poisson_solver.argtypes = [_dp, _dp, C.c_int, C.c_int, C.c_int, C.c_double, C.POINTER(C.c_double)]
         L.pcdo_poisson_solver.restype = C.c_int
+        L.pcdo_poisson_solver_threads.argtypes = [_dp, _dp, C.c_int, C.c_int, C.c_int, C.c_double, C.c_int,
+                                                  C.c_int, C.c_double, C.POINTER(C.c_double)]
+        L.pcdo_poisson_solver_threads.restype = C.c_int
         L.pcdo_sor_sweeps.argtypes = [_dp, _dp, C.c_int, C.c_int, C.c_int, C.c_double]
         L.pcdo_sor_sweeps.restype = C.c_double
         L.pcdo_residual.argtypes = [_dp, _dp, C.c_int, C.c_int, C.c_void_p, _dp]
@@ -89,6 +92,17 @@ class Port:
         h, w = D.shape
         mu = C.c_double(0)
         n = self.L.pcdo_poisson_solver(D, phi, w, h, int(max_iterations), float(tol), C.byref(mu))
+        return n, mu.value
+
+    def poisson_solver_threads(self, D, phi, max_iterations=100000, tol=1e-7, max_threads=1, omega=0.0):
+        """solver.cpp:70-148 with the reference's tile threading (hardware
+        threads = os.cpu_count()).  Returns (sweeps, last max|delta|)."""
+        D = _f64(D)
+        assert phi.dtype == np.float64 and phi.flags.c_contiguous
+        h, w = D.shape
+        mu = C.c_double(0)
+        n = self.L.pcdo_poisson_solver_threads(D, phi, w, h, int(max_iterations), float(tol), int(max_threads),
+                                               int(os.cpu_count() or 1), float(omega), C.byref(mu))
         return n, mu.value
 
     def sor_sweeps(self, D, phi, sweeps, omega=None):

@@ -20,6 +20,7 @@
  * vector<vector<double>> g[y][x]); mesh points are n x 3 arrays (x, y, z).
  */
 #include <math.h>
+#include <pthread.h>
 #include <stdlib.h>
 #include <string.h>
 
@@ -66,6 +67,78 @@ int pcdo_poisson_solver(const double *b, double *phi, int w, int h, int max_iter
         sweeps = i + 1;
         if (mu < tol) break;                                /* solver.cpp:142 */
     }
+    if (last_max_update) *last_max_update = mu;
+    return sweeps;
+}
+
+/* The reference's threaded schedule, solver.cpp:70-148 with max_threads = T:
+ * ceil/floor tiles on a floor(sqrt(min(T, hardware threads)))^2 grid
+ * (:73-83, :121-131), one thread spawned per tile and joined every sweep, the
+ * sweep's max |delta| taken under a mutex (:104-118).  Tiles read their
+ * neighbours' boundary cells while those are being written, exactly like the
+ * reference (chaotic relaxation), so results with T >= 4 are not bit-stable.
+ * Returns the number of sweeps run. */
+struct tile_job {
+    double *phi;
+    const double *b;
+    int w, h, x0, y0, x1, y1;
+    double omega;
+    double *max_update;
+    pthread_mutex_t *mtx;
+};
+
+static void *tile_worker(void *arg)
+{
+    struct tile_job *j = (struct tile_job *)arg;
+    double m = relax_tile(j->phi, j->b, j->w, j->h, j->omega, j->x0, j->y0, j->x1, j->y1);
+    pthread_mutex_lock(j->mtx);
+    if (*j->max_update < m) *j->max_update = m;
+    pthread_mutex_unlock(j->mtx);
+    return NULL;
+}
+
+int pcdo_poisson_solver_threads(const double *b, double *phi, int w, int h, int max_iterations, double tol,
+                                int max_threads, int hw_threads, double omega, double *last_max_update)
+{
+    if (omega <= 0.0) omega = 2.0 / (1.0 + 3.14159265 / w);   /* solver.cpp:71 */
+    int nt = max_threads < hw_threads ? max_threads : hw_threads;
+    int seg = (int)floor(sqrt((double)nt));
+    if (seg < 1) seg = 1;
+    int ntiles = seg * seg;
+    struct tile_job *jobs = (struct tile_job *)malloc(sizeof(struct tile_job) * ntiles);
+    pthread_t *th = (pthread_t *)malloc(sizeof(pthread_t) * ntiles);
+    pthread_mutex_t mtx;
+    pthread_mutex_init(&mtx, NULL);
+    double mu = 0.0;
+    int sweeps = 0;
+    for (int i = 0; i < max_iterations; i++) {
+        double max_update = 0.0;
+        for (int ty = 0; ty < seg; ty++)
+            for (int tx = 0; tx < seg; tx++) {
+                struct tile_job *j = &jobs[ty * seg + tx];
+                j->phi = phi; j->b = b; j->w = w; j->h = h; j->omega = omega;
+                j->x0 = (int)floor((double)tx * ((double)w / (double)seg));
+                j->y0 = (int)floor((double)ty * ((double)h / (double)seg));
+                j->x1 = (int)ceil((double)(tx + 1) * ((double)w / (double)seg));
+                j->y1 = (int)ceil((double)(ty + 1) * ((double)h / (double)seg));
+                if (j->x1 > w) j->x1 = w;
+                if (j->y1 > h) j->y1 = h;
+                j->max_update = &max_update;
+                j->mtx = &mtx;
+            }
+        if (ntiles == 1) {
+            tile_worker(&jobs[0]);
+        } else {
+            for (int k = 0; k < ntiles; k++) pthread_create(&th[k], NULL, tile_worker, &jobs[k]);
+            for (int k = 0; k < ntiles; k++) pthread_join(th[k], NULL);
+        }
+        mu = max_update;
+        sweeps = i + 1;
+        if (max_update < tol) break;
+    }
+    pthread_mutex_destroy(&mtx);
+    free(jobs);
+    free(th);
     if (last_max_update) *last_max_update = mu;
     return sweeps;
 }

@@ -1,0 +1,153 @@
+"""Host mirror of ``class Caustic_design`` (src/caustic_design.h:7-66).
+
+Method names, argument meaning and call order follow the reference:
+
+    d = CausticDesign()
+    d.set_mesh_resolution(res, res)            # caustic_design.cpp:28-31
+    d.set_domain_resolution(4*res, 4*res)      # :33-36
+    d.set_mesh_size(width, height)             # :38-41
+    d.set_lens_focal_length(focal)             # :43-45
+    d.set_lens_thickness(thickness)            # :47-49
+    d.set_solver_max_threads(n)                # :51-53 (accepted, ignored)
+    d.initialize_solvers(image)                # :334-364
+    step = d.perform_transport_iteration()     # :190-266
+    d.perform_height_map_iteration(itr)        # :269-332
+
+The state lives on the GPU (libpcd_gb300); the reference's public members
+(``phi``, ``h``, ``raster``, ``errors``, ``mesh->target_points`` ...) are
+read through properties that copy them to host arrays on access.  A raster
+miss raises ``PCDError`` with status PCD_RASTER_MISS (the reference calls
+exit(0), mesh.cpp:277-279).
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib
+from ._lib import check
+from .solver import Context, SolveOptions
+
+GRID = {"phi": 0, "h": 1, "raster": 2, "divergence": 3, "norm_x": 4, "norm_y": 5}
+VERT = {"target_points": 10, "source_points": 11, "target_areas": 12, "errors": 13, "normals_x": 14,
+        "normals_y": 15, "vertex_gradient_x": 16, "vertex_gradient_y": 17}
+
+
+class CausticDesign:
+    def __init__(self, ctx: Context | None = None, transport: SolveOptions | None = None,
+                 height_solve: SolveOptions | None = None):
+        self._L = _lib.load()
+        self._ctx = ctx or Context()
+        self._own_ctx = ctx is None
+        self._h = None
+        self.mesh_res_x = self.mesh_res_y = 0
+        self.resolution_x = self.resolution_y = 0
+        self.width = self.height = 0.0
+        self.focal_l = self.thickness = 0.0
+        self.nthreads = 0
+        self.transport_opts = transport or SolveOptions(tol=1e-7)      # caustic_design.cpp:222
+        self.height_opts = height_solve or SolveOptions(tol=1e-8)      # caustic_design.cpp:311
+        self.last_solve_stats = None
+
+    # ---- setters (caustic_design.cpp:28-53) ----
+    def set_mesh_resolution(self, width: int, height: int):
+        self.mesh_res_x, self.mesh_res_y = int(width), int(height)
+
+    def set_domain_resolution(self, width: int, height: int):
+        self.resolution_x, self.resolution_y = int(width), int(height)
+
+    def set_mesh_size(self, width: float, height: float):
+        self.width, self.height = float(width), float(height)
+
+    def set_lens_focal_length(self, focal_length: float):
+        self.focal_l = float(focal_length)
+
+    def set_lens_thickness(self, thickness: float):
+        self.thickness = float(thickness)
+
+    def set_solver_max_threads(self, n_threads: int):
+        self.nthreads = int(n_threads)
+
+    # ---- iterations ----
+    def initialize_solvers(self, image):
+        img = np.ascontiguousarray(image, dtype=np.float64)
+        if img.shape != (self.resolution_y, self.resolution_x):
+            raise ValueError(f"image must be resolution_y x resolution_x = {(self.resolution_y, self.resolution_x)}")
+        self.close()
+        p = _lib.DesignParams()
+        self._L.pcd_design_params_default(C.byref(p))
+        p.mesh_res_x, p.mesh_res_y = self.mesh_res_x, self.mesh_res_y
+        p.res_x, p.res_y = self.resolution_x, self.resolution_y
+        p.width, p.height = self.width, self.height
+        p.focal_l, p.thickness = self.focal_l, self.thickness
+        p.transport = self.transport_opts.to_c()
+        p.height_solve = self.height_opts.to_c()
+        h = C.c_void_p()
+        check(self._L.pcd_design_create(self._ctx.handle, C.byref(p), C.byref(h)), "pcd_design_create")
+        self._h = h
+        check(self._L.pcd_design_initialize(self._h, img.ctypes.data), "pcd_design_initialize")
+
+    def perform_transport_iteration(self) -> float:
+        step = C.c_double(0)
+        st = _lib.SolveStats()
+        check(self._L.pcd_design_transport_iteration(self._h, C.byref(step), C.byref(st)),
+              "pcd_design_transport_iteration")
+        self.last_solve_stats = st.as_dict()
+        return step.value
+
+    def perform_height_map_iteration(self, itr: int = 0) -> float:
+        upd = C.c_double(0)
+        st = _lib.SolveStats()
+        check(self._L.pcd_design_height_iteration(self._h, int(itr), C.byref(upd), C.byref(st)),
+              "pcd_design_height_iteration")
+        self.last_solve_stats = st.as_dict()
+        return upd.value
+
+    # ---- public members (caustic_design.h:16-30, mesh.h:51-52) ----
+    def _grid(self, name):
+        out = np.empty((self.resolution_y, self.resolution_x))
+        check(self._L.pcd_design_get_grid(self._h, GRID[name], out.ctypes.data), "pcd_design_get_grid")
+        return out
+
+    def _vert(self, name):
+        n = self.mesh_res_x * self.mesh_res_y
+        out = np.empty((n, 3)) if name.endswith("points") else np.empty(n)
+        check(self._L.pcd_design_get_vertices(self._h, VERT[name], out.ctypes.data), "pcd_design_get_vertices")
+        return out
+
+    phi = property(lambda self: self._grid("phi"))
+    h = property(lambda self: self._grid("h"))
+    raster = property(lambda self: self._grid("raster"))
+    divergence = property(lambda self: self._grid("divergence"))
+    norm_x = property(lambda self: self._grid("norm_x"))
+    norm_y = property(lambda self: self._grid("norm_y"))
+    errors = property(lambda self: self._vert("errors"))
+    target_areas = property(lambda self: self._vert("target_areas"))
+
+    @property
+    def vertex_gradient(self):
+        return [self._vert("vertex_gradient_x"), self._vert("vertex_gradient_y")]
+
+    @property
+    def normals(self):
+        return [self._vert("normals_x"), self._vert("normals_y")]
+
+    def target_points(self):
+        return self._vert("target_points")
+
+    def source_points(self):
+        return self._vert("source_points")
+
+    def close(self):
+        if self._h:
+            self._L.pcd_design_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+            if self._own_ctx:
+                self._ctx.close()
+        except Exception:
+            pass

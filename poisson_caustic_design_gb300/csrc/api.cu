@@ -1,0 +1,231 @@
+// api.cu -- C ABI of libpcd_gb300: context, Poisson solve, grid utilities.
+//
+// Declarations and the reference interfaces they replace: include/pcd.h.
+#include <atomic>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+
+#include "api_internal.cuh"
+#include "design.cuh"
+
+namespace pcd {
+
+namespace {
+thread_local std::string g_last_error;
+std::atomic<unsigned long long> g_launches{0};
+}  // namespace
+
+void set_error(const std::string &msg) { g_last_error = msg; }
+void count_launches(unsigned long long n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+
+int ctx_stage(pcd_ctx *ctx, size_t cells)
+{
+    if (cells > ctx->host_cells) {
+        if (ctx->d_b) cudaFree(ctx->d_b);
+        if (ctx->d_phi) cudaFree(ctx->d_phi);
+        ctx->d_b = nullptr;
+        ctx->d_phi = nullptr;
+        ctx->host_cells = 0;
+        PCD_CUDA(cudaMalloc(&ctx->d_b, cells * sizeof(double)));
+        PCD_CUDA(cudaMalloc(&ctx->d_phi, cells * sizeof(double)));
+        ctx->host_cells = cells;
+    }
+    return PCD_OK;
+}
+
+int ctx_activate(pcd_ctx *ctx)
+{
+    PCD_CUDA(cudaSetDevice(ctx->device));
+    return PCD_OK;
+}
+
+}  // namespace pcd
+
+using namespace pcd;
+
+extern "C" {
+
+const char *pcd_last_error(void) { return g_last_error.c_str(); }
+
+unsigned long long pcd_kernel_launches(void) { return g_launches.load(); }
+
+const char *pcd_status_string(int status)
+{
+    switch (status) {
+    case PCD_OK: return "ok";
+    case PCD_NOT_CONVERGED: return "not converged";
+    case PCD_BAD_ARG: return "bad argument";
+    case PCD_DEVICE_ERROR: return "device error";
+    case PCD_TIMEOUT: return "timeout";
+    case PCD_RASTER_MISS: return "raster miss";
+    case PCD_NO_DEVICE: return "no CUDA device";
+    case PCD_FALLBACK_USED: return "fallback used";
+    }
+    return "unknown status";
+}
+
+int pcd_solve_opts_default(pcd_solve_opts *o)
+{
+    if (!o) return PCD_BAD_ARG;
+    std::memset(o, 0, sizeof(*o));
+    o->max_iterations = 100000;   // caustic_design.cpp:222,311
+    o->tol = 1e-7;                // caustic_design.cpp:222
+    o->stop = PCD_STOP_MAX_UPDATE;
+    o->precision = PCD_PREC_FP64;
+    o->omega = 0.0;
+    o->check_every = 0;
+    o->refine_every = 0;
+    o->warm_start = 1;
+    o->schedule = PCD_SCHED_AUTO;
+    return PCD_OK;
+}
+
+int pcd_ctx_create(int device, pcd_ctx **out)
+{
+    if (!out) return PCD_BAD_ARG;
+    *out = nullptr;
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess || n == 0) {
+        set_error(std::string("no CUDA device: ") + cudaGetErrorString(e));
+        return PCD_NO_DEVICE;
+    }
+    if (device < 0) PCD_CUDA(cudaGetDevice(&device));
+    if (device >= n) {
+        set_error("pcd_ctx_create: device index out of range");
+        return PCD_BAD_ARG;
+    }
+    PCD_CUDA(cudaSetDevice(device));
+    auto *c = new pcd_ctx();
+    c->device = device;
+    c->solver.dev = device;
+    cudaError_t ce = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    if (ce != cudaSuccess) {
+        delete c;
+        set_error(std::string("cudaStreamCreate: ") + cudaGetErrorString(ce));
+        return PCD_DEVICE_ERROR;
+    }
+    *out = c;
+    return PCD_OK;
+}
+
+int pcd_ctx_destroy(pcd_ctx *ctx)
+{
+    if (!ctx) return PCD_OK;
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    design_detach_all(ctx);
+    ctx->solver.release();
+    ctx->grid.release();
+    if (ctx->d_b) cudaFree(ctx->d_b);
+    if (ctx->d_phi) cudaFree(ctx->d_phi);
+    cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return PCD_OK;
+}
+
+void *pcd_ctx_stream(pcd_ctx *ctx) { return ctx ? (void *)ctx->stream : nullptr; }
+
+int pcd_poisson_solve_device(pcd_ctx *ctx, const double *b, double *phi, int width, int height, int ld,
+                             const pcd_solve_opts *opts, pcd_solve_stats *stats, void *stream)
+{
+    if (!ctx) return PCD_BAD_ARG;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    PCD_TRY(ctx_activate(ctx));
+    pcd_solve_opts o;
+    if (opts) o = *opts; else pcd_solve_opts_default(&o);
+    cudaStream_t s = stream ? (cudaStream_t)stream : ctx->stream;
+    return solve_device(ctx->solver, b, phi, width, height, ld, o, stats, s);
+}
+
+int pcd_poisson_solve(pcd_ctx *ctx, const double *b, double *phi, int width, int height,
+                      const pcd_solve_opts *opts, pcd_solve_stats *stats)
+{
+    if (!ctx || !b || !phi || width < 1 || height < 1) {
+        set_error("pcd_poisson_solve: bad arguments");
+        return PCD_BAD_ARG;
+    }
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    PCD_TRY(ctx_activate(ctx));
+    pcd_solve_opts o;
+    if (opts) o = *opts; else pcd_solve_opts_default(&o);
+    const size_t n = (size_t)width * height;
+    PCD_TRY(ctx_stage(ctx, n));
+    cudaStream_t s = ctx->stream;
+    PCD_CUDA(cudaMemcpyAsync(ctx->d_b, b, n * sizeof(double), cudaMemcpyHostToDevice, s));
+    if (o.warm_start) PCD_CUDA(cudaMemcpyAsync(ctx->d_phi, phi, n * sizeof(double), cudaMemcpyHostToDevice, s));
+    int st = solve_device(ctx->solver, ctx->d_b, ctx->d_phi, width, height, width, o, stats, s);
+    if (st != PCD_OK && st != PCD_NOT_CONVERGED) return st;
+    PCD_CUDA(cudaMemcpyAsync(phi, ctx->d_phi, n * sizeof(double), cudaMemcpyDeviceToHost, s));
+    PCD_CUDA(cudaStreamSynchronize(s));
+    return st;
+}
+
+// Process-wide contexts for the reference-shaped entry point, one per device.
+static std::mutex g_default_mu;
+static std::map<int, pcd_ctx *> g_default;
+
+static int default_ctx(pcd_ctx **out)
+{
+    int dev = 0;
+    PCD_CUDA(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lk(g_default_mu);
+    auto it = g_default.find(dev);
+    if (it != g_default.end()) {
+        *out = it->second;
+        return PCD_OK;
+    }
+    pcd_ctx *c = nullptr;
+    PCD_TRY(pcd_ctx_create(dev, &c));
+    g_default[dev] = c;
+    *out = c;
+    return PCD_OK;
+}
+
+int pcd_poisson_solver(const double *D, double *phi, int width, int height, int max_iterations,
+                       double convergence_threshold, int max_threads)
+{
+    (void)max_threads;  // the reference splits each sweep over threads; one GPU here
+    pcd_ctx *ctx = nullptr;
+    PCD_TRY(default_ctx(&ctx));
+    pcd_solve_opts o;
+    pcd_solve_opts_default(&o);
+    o.max_iterations = max_iterations;
+    o.tol = convergence_threshold;
+    o.stop = PCD_STOP_MAX_UPDATE;
+    o.precision = PCD_PREC_FP64;
+    o.warm_start = 1;
+    return pcd_poisson_solve(ctx, D, phi, width, height, &o, nullptr);
+}
+
+int pcd_subtract_average_device(pcd_ctx *ctx, double *g, int width, int height, void *stream)
+{
+    if (!ctx || !g || width < 1 || height < 1) return PCD_BAD_ARG;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    PCD_TRY(ctx_activate(ctx));
+    return subtract_average(ctx->grid, g, (long)width * height, stream ? (cudaStream_t)stream : ctx->stream);
+}
+
+int pcd_gradient_device(pcd_ctx *ctx, const double *g, double *gx, double *gy, int width, int height,
+                        void *stream)
+{
+    if (!ctx || !g || !gx || !gy || width < 1 || height < 1) return PCD_BAD_ARG;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    PCD_TRY(ctx_activate(ctx));
+    return gradient(g, gx, gy, width, height, stream ? (cudaStream_t)stream : ctx->stream);
+}
+
+int pcd_divergence_device(pcd_ctx *ctx, const double *nx, const double *ny, double *div, int width, int height,
+                          void *stream)
+{
+    if (!ctx || !nx || !ny || !div || width < 1 || height < 1) return PCD_BAD_ARG;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    PCD_TRY(ctx_activate(ctx));
+    return divergence(nx, ny, div, width, height, stream ? (cudaStream_t)stream : ctx->stream);
+}
+
+}  // extern "C"

@@ -1,0 +1,764 @@
+// solver.cu -- red-black SOR for the reference's Poisson problem on sm_103a.
+//
+// Reference: poisson_solver / patial_relax, src/solver.cpp:12-148.  The
+// reference relaxes lexicographically (Gauss-Seidel order) with
+// omega = 2/(1+pi/width) and stops when one sweep's max |delta| drops below a
+// threshold.  Here every sweep is two half sweeps over the red ((x+y) even)
+// and black cells, which have no neighbours of their own colour, so each half
+// sweep is one fully parallel kernel.  Red-black SOR with the same omega has
+// the same asymptotic rate as the lexicographic ordering (both are consistent
+// orderings); intermediate iterates differ, the fixed point is the same.
+//
+// Two stop tests: the reference's max |delta| (checked after every sweep by
+// the last block of the black half sweep) and a relative FP64 residual
+// ||b - L phi|| / ||b|| checked every `check_every` sweeps.
+//
+// Two precisions: FP64 sweeps on phi, or FP32 sweeps on the error equation
+// L e = r with the residual r = b - L(phi + e) and the update phi += e done in
+// FP64 every `refine_every` sweeps (defect correction).  SOR is a stationary
+// iteration, so restarting it on the refreshed residual from e = 0 changes
+// nothing in exact arithmetic; FP32 only limits how far e may be pushed
+// between refreshes.
+//
+// Sweeps are issued as CUDA-graph chunks; the stop flags live in device memory
+// and make the remaining kernels of a chunk return at once, so the host reads
+// the control block once per chunk and launches the next chunk speculatively.
+#include <cmath>
+#include <cstring>
+
+#include "solver.cuh"
+#include "sor_persist.cuh"
+#include "sor_cluster.cuh"
+
+namespace pcd {
+
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int kResidualBlocksMax = 1216;  // 152 SMs x 8
+
+__device__ __forceinline__ int vol_load(const int *p) { return *(volatile const int *)p; }
+
+// ---------------------------------------------------------------------------
+// Neighbour-validity mask: bit0 left, bit1 up, bit2 right, bit3 down (inside
+// the grid and b not NaN, solver.cpp:29-44); bit4 set when b itself is NaN.
+// ---------------------------------------------------------------------------
+__global__ void k_mask(const double *__restrict__ b, uint8_t *__restrict__ mask, int W, int H, int ld,
+                       Ctl *ctl)
+{
+    long n = (long)W * H;
+    int nan_local = 0;
+    for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x) {
+        int y = (int)(t / W), x = (int)(t - (long)y * W);
+        long i = (long)y * ld + x;
+        uint8_t m = 0;
+        if (x > 0 && !isnan(b[i - 1])) m |= 1;
+        if (y > 0 && !isnan(b[i - ld])) m |= 2;
+        if (x < W - 1 && !isnan(b[i + 1])) m |= 4;
+        if (y < H - 1 && !isnan(b[i + ld])) m |= 8;
+        if (isnan(b[i])) { m |= 16; nan_local++; }
+        mask[i] = m;
+    }
+    if (nan_local) atomicAdd(&ctl->nan_cells, nan_local);
+}
+
+template <typename T, bool MASKED>
+__device__ __forceinline__ void gather(const T *__restrict__ phi, const uint8_t *__restrict__ mask, long i, int x,
+                                       int y, int W, int H, int ld, T &sum, T &cnt)
+{
+    sum = T(0);
+    cnt = T(0);
+    if (MASKED) {
+        const uint8_t m = mask[i];
+        if (m & 1) { cnt += T(1); sum += phi[i - 1]; }
+        if (m & 2) { cnt += T(1); sum += phi[i - ld]; }
+        if (m & 4) { cnt += T(1); sum += phi[i + 1]; }
+        if (m & 8) { cnt += T(1); sum += phi[i + ld]; }
+    } else {
+        if (x > 0) { cnt += T(1); sum += phi[i - 1]; }
+        if (y > 0) { cnt += T(1); sum += phi[i - ld]; }
+        if (x < W - 1) { cnt += T(1); sum += phi[i + 1]; }
+        if (y < H - 1) { cnt += T(1); sum += phi[i + ld]; }
+    }
+}
+
+// omega/cnt from the host-divided table, selected without dynamic indexing
+// (which would place the argument struct in local memory).
+template <typename T>
+__device__ __forceinline__ T omega_over_cnt(const SolveArgs &a, int cnt)
+{
+    if (sizeof(T) == 8)
+        return (T)(cnt == 4 ? a.w64[4] : cnt == 3 ? a.w64[3] : cnt == 2 ? a.w64[2] : cnt == 1 ? a.w64[1] : a.w64[0]);
+    return (T)(cnt == 4 ? a.w32[4] : cnt == 3 ? a.w32[3] : cnt == 2 ? a.w32[2] : cnt == 1 ? a.w32[1] : a.w32[0]);
+}
+
+// End-of-sweep bookkeeping, run by the last block of the black half sweep.
+__device__ void end_of_sweep(Ctl *ctl, const SolveArgs &a)
+{
+    volatile Ctl *c = ctl;
+    unsigned long long bits = atomicExch(&ctl->maxbits, 0ull);
+    double mx = __longlong_as_double((long long)bits);
+    c->last_max = mx;
+    int s = c->sweeps + 1;
+    c->sweeps = s;
+    if (a.stop == PCD_STOP_MAX_UPDATE && mx < a.tol) {
+        c->converged = 1;
+        c->halt = 1;
+    }
+    if (s >= a.max_iter) c->halt = 1;
+    c->blocks_done = 0;
+    __threadfence();
+}
+
+// One half sweep over the cells of `color`: delta = omega/cnt*(sum - cnt*v - b)
+// (solver.cpp:47), phi += delta.  TRACK keeps the sweep's max |delta|.
+template <typename T, bool MASKED, bool TRACK>
+__global__ void __launch_bounds__(kThreads)
+    k_rb_half(T *__restrict__ phi, const T *__restrict__ rhs, const uint8_t *__restrict__ mask, Ctl *ctl,
+              SolveArgs a, int color, int last_half)
+{
+    if (vol_load(&ctl->halt)) return;
+    const int half = (a.W + 1) >> 1;
+    const long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    double m = 0.0;
+    if (idx < (long)a.H * half) {
+        const int y = (int)(idx / half);
+        const int x = 2 * (int)(idx - (long)y * half) + ((y + color) & 1);
+        if (x < a.W) {
+            const long i = (long)y * a.ld + x;
+            T sum, cnt;
+            gather<T, MASKED>(phi, mask, i, x, y, a.W, a.H, a.ld, sum, cnt);
+            const T v = phi[i];
+            const T w = omega_over_cnt<T>(a, (int)cnt);
+            const T delta = w * (sum - cnt * v - rhs[i]);
+            phi[i] = v + delta;
+            if (TRACK) {
+                double ad = fabs((double)delta);
+                m = ad > 0.0 ? ad : 0.0;  // NaN deltas never raise the max (solver.cpp:51)
+            }
+        }
+    }
+    if (!TRACK && !last_half) return;
+    if (TRACK) {
+        double v[1] = {m};
+        block_reduce<1, 1u>(v);
+        m = v[0];
+    }
+    if (threadIdx.x == 0) {
+        if (TRACK && m > 0.0) atomicMax(&ctl->maxbits, (unsigned long long)__double_as_longlong(m));
+        if (last_half) {
+            __threadfence();
+            unsigned t = atomicAdd(&ctl->blocks_done, 1u);
+            if (t == gridDim.x - 1) {
+                __threadfence();
+                end_of_sweep(ctl, a);
+            }
+        }
+    }
+}
+
+// Last-block finalisation of a residual reduction: sums the per-block
+// partials in a fixed order (deterministic), stores the norms and applies the
+// relative-residual stop test when `test` is set.
+__device__ void finalize_residual(Ctl *ctl, const double *partials, int nblk, const SolveArgs &a, int test,
+                                  int with_b)
+{
+    double v[3] = {0.0, 0.0, 0.0};
+    for (int k = threadIdx.x; k < nblk; k += blockDim.x) {
+        v[0] += partials[3 * k];
+        v[1] += partials[3 * k + 1];
+        v[2] = fmax(v[2], partials[3 * k + 2]);
+    }
+    block_reduce<3, 4u>(v);
+    if (threadIdx.x == 0) {
+        volatile Ctl *c = ctl;
+        double rn = sqrt(v[0]);
+        if (with_b) c->bnorm = sqrt(v[1]);
+        double bn = c->bnorm;
+        c->rnorm = rn;
+        c->rmax = v[2];
+        double rel = bn > 0.0 ? rn / bn : rn;
+        c->rel = rel;
+        c->checks = c->checks + 1;
+        if (test && a.stop == PCD_STOP_REL_RESIDUAL && rel <= a.tol) {
+            c->converged = 1;
+            c->halt = 1;
+        }
+        c->blocks_done_r = 0;
+        __threadfence();
+    }
+}
+
+__device__ __forceinline__ bool last_block(Ctl *ctl)
+{
+    __shared__ bool is_last;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        unsigned t = atomicAdd(&ctl->blocks_done_r, 1u);
+        is_last = (t == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (is_last) __threadfence();
+    return is_last;
+}
+
+// FP64 residual r = b - L phi over non-NaN cells; partial sums of r^2, b^2
+// and max |r|.  `test`: apply the stop test (loop checks); `skip_halted`:
+// return at once when the solve already halted.
+template <bool MASKED>
+__global__ void __launch_bounds__(kThreads)
+    k_residual64(const double *__restrict__ phi, const double *__restrict__ b, const uint8_t *__restrict__ mask,
+                 Ctl *ctl, double *partials, SolveArgs a, int test, int with_b, int skip_halted,
+                 double *__restrict__ rout = nullptr)
+{
+    if (skip_halted && vol_load(&ctl->halt)) return;
+    const long n = (long)a.W * a.H;
+    double v[3] = {0.0, 0.0, 0.0};
+    for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x) {
+        const int y = (int)(t / a.W), x = (int)(t - (long)y * a.W);
+        const long i = (long)y * a.ld + x;
+        const double bi = b[i];
+        if (isnan(bi)) continue;
+        double sum, cnt;
+        gather<double, MASKED>(phi, mask, i, x, y, a.W, a.H, a.ld, sum, cnt);
+        const double r = bi - (sum - cnt * phi[i]);
+        if (rout) rout[i] = r;
+        v[0] += r * r;
+        v[1] += bi * bi;
+        v[2] = nan_skip_max(v[2], fabs(r));
+    }
+    block_reduce<3, 4u>(v);
+    if (threadIdx.x == 0) {
+        partials[3 * blockIdx.x] = v[0];
+        partials[3 * blockIdx.x + 1] = v[1];
+        partials[3 * blockIdx.x + 2] = v[2];
+    }
+    if (last_block(ctl)) finalize_residual(ctl, partials, gridDim.x, a, test, with_b);
+}
+
+// Mixed precision: r = b - L(phi + e) in FP64 (e widened exactly), written to
+// r32 as the next right-hand side of the FP32 correction sweeps.
+template <bool MASKED>
+__global__ void __launch_bounds__(kThreads)
+    k_refine_residual(const double *__restrict__ phi, const float *__restrict__ e, const double *__restrict__ b,
+                      const uint8_t *__restrict__ mask, float *__restrict__ r32, Ctl *ctl, double *partials,
+                      SolveArgs a, int with_b)
+{
+    if (vol_load(&ctl->done)) return;
+    const long n = (long)a.W * a.H;
+    double v[3] = {0.0, 0.0, 0.0};
+    for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x) {
+        const int y = (int)(t / a.W), x = (int)(t - (long)y * a.W);
+        const long i = (long)y * a.ld + x;
+        const double bi = b[i];
+        double sum = 0.0, cnt = 0.0;
+        if (MASKED) {
+            const uint8_t m = mask[i];
+            if (m & 1) { cnt += 1.0; sum += phi[i - 1] + (double)e[i - 1]; }
+            if (m & 2) { cnt += 1.0; sum += phi[i - a.ld] + (double)e[i - a.ld]; }
+            if (m & 4) { cnt += 1.0; sum += phi[i + 1] + (double)e[i + 1]; }
+            if (m & 8) { cnt += 1.0; sum += phi[i + a.ld] + (double)e[i + a.ld]; }
+        } else {
+            if (x > 0) { cnt += 1.0; sum += phi[i - 1] + (double)e[i - 1]; }
+            if (y > 0) { cnt += 1.0; sum += phi[i - a.ld] + (double)e[i - a.ld]; }
+            if (x < a.W - 1) { cnt += 1.0; sum += phi[i + 1] + (double)e[i + 1]; }
+            if (y < a.H - 1) { cnt += 1.0; sum += phi[i + a.ld] + (double)e[i + a.ld]; }
+        }
+        const double xi = phi[i] + (double)e[i];
+        const double r = bi - (sum - cnt * xi);
+        r32[i] = (float)r;
+        if (isnan(bi)) continue;
+        v[0] += r * r;
+        v[1] += bi * bi;
+        v[2] = nan_skip_max(v[2], fabs(r));
+    }
+    block_reduce<3, 4u>(v);
+    if (threadIdx.x == 0) {
+        partials[3 * blockIdx.x] = v[0];
+        partials[3 * blockIdx.x + 1] = v[1];
+        partials[3 * blockIdx.x + 2] = v[2];
+    }
+    if (last_block(ctl)) finalize_residual(ctl, partials, gridDim.x, a, 1, with_b);
+}
+
+// Mixed precision: phi += e, e = 0.  The last block marks the solve done once
+// the sweeps have halted (the correction that halted them is now in phi).
+__global__ void __launch_bounds__(kThreads)
+    k_refine_update(double *__restrict__ phi, float *__restrict__ e, Ctl *ctl, SolveArgs a)
+{
+    if (vol_load(&ctl->done)) return;
+    const long n = (long)a.W * a.H;
+    for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x) {
+        const int y = (int)(t / a.W), x = (int)(t - (long)y * a.W);
+        const long i = (long)y * a.ld + x;
+        phi[i] += (double)e[i];
+        e[i] = 0.0f;
+    }
+    if (last_block(ctl)) {
+        if (threadIdx.x == 0) {
+            volatile Ctl *c = ctl;
+            if (c->halt) c->done = 1;
+            c->blocks_done_r = 0;
+            __threadfence();
+        }
+    }
+}
+
+__global__ void k_fill(double *p, int W, int H, int ld, double v)
+{
+    const long n = (long)W * H;
+    for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x) {
+        const int y = (int)(t / W), x = (int)(t - (long)y * W);
+        p[(long)y * ld + x] = v;
+    }
+}
+
+inline int grid_blocks(long n) { return (int)std::min<long>(kResidualBlocksMax, (n + kThreads - 1) / kThreads); }
+
+}  // namespace
+
+double resolve_omega(double omega, int W, int H)
+{
+    if (omega > 0.0) return omega;
+    if (omega == 0.0) return 2.0 / (1.0 + 3.14159265 / W);  // solver.cpp:71
+    const int n = W > H ? W : H;
+    if (n < 2) return 1.0;
+    const double mu = 0.5 * (1.0 + std::cos(M_PI / n));
+    return 2.0 / (1.0 + std::sqrt(1.0 - mu * mu));
+}
+
+int SolverWorkspace::reserve(size_t n)
+{
+    if (!ctl) {
+        PCD_CUDA(cudaMalloc(&ctl, sizeof(Ctl)));
+        PCD_CUDA(cudaMallocHost(&ctl_host, 2 * sizeof(Ctl)));
+        PCD_CUDA(cudaMalloc(&partials, 3 * sizeof(double) * kResidualBlocksMax));
+        max_partials = kResidualBlocksMax;
+        for (int k = 0; k < 2; k++) PCD_CUDA(cudaEventCreateWithFlags(&ev[k], cudaEventDisableTiming));
+        PCD_CUDA(cudaEventCreate(&t0));
+        PCD_CUDA(cudaEventCreate(&t1));
+        PCD_CUDA(cudaEventCreate(&k0));
+        PCD_CUDA(cudaEventCreate(&k1));
+    }
+    if (n > cells) {
+        if (mask) cudaFree(mask);
+        if (e32) cudaFree(e32);
+        if (r32) cudaFree(r32);
+        if (r64) cudaFree(r64);
+        mask = nullptr; e32 = nullptr; r32 = nullptr; r64 = nullptr;
+        for (auto &kv : graphs) cudaGraphExecDestroy(kv.second.exec);
+        graphs.clear();
+        PCD_CUDA(cudaMalloc(&mask, n));
+        PCD_CUDA(cudaMalloc(&e32, n * sizeof(float)));
+        PCD_CUDA(cudaMalloc(&r32, n * sizeof(float)));
+        PCD_CUDA(cudaMalloc(&r64, n * sizeof(double)));
+        cells = n;
+    }
+    return PCD_OK;
+}
+
+void SolverWorkspace::release()
+{
+    for (auto &kv : graphs) cudaGraphExecDestroy(kv.second.exec);
+    graphs.clear();
+    if (mask) cudaFree(mask);
+    if (e32) cudaFree(e32);
+    if (r32) cudaFree(r32);
+    if (r64) cudaFree(r64);
+    if (xbuf) cudaFree(xbuf);
+    if (flags) cudaFree(flags);
+    if (part) cudaFree(part);
+    r64 = nullptr; xbuf = nullptr; flags = nullptr; part = nullptr;
+    xbuf_elems = 0; max_ctas = 0;
+    if (partials) cudaFree(partials);
+    if (ctl) cudaFree(ctl);
+    if (ctl_host) cudaFreeHost(ctl_host);
+    for (int k = 0; k < 2; k++)
+        if (ev[k]) cudaEventDestroy(ev[k]);
+    if (t0) cudaEventDestroy(t0);
+    if (t1) cudaEventDestroy(t1);
+    if (k0) cudaEventDestroy(k0);
+    if (k1) cudaEventDestroy(k1);
+    mask = nullptr; e32 = nullptr; r32 = nullptr; partials = nullptr; ctl = nullptr; ctl_host = nullptr;
+    cells = 0;
+}
+
+namespace {
+
+// Enqueues one chunk of `sweeps` sweeps (plus the checks that follow them) on s.
+template <bool MASKED>
+int enqueue_chunk(SolverWorkspace &ws, const double *b, double *phi, const SolveArgs &a, int precision,
+                  int sweeps, cudaStream_t s, int *nodes)
+{
+    const int half = (a.W + 1) >> 1;
+    const int blocks = ceil_div((long)a.H * half, kThreads);
+    const int rblocks = grid_blocks((long)a.W * a.H);
+    const bool track = (a.stop == PCD_STOP_MAX_UPDATE);
+    int n = 0;
+    for (int k = 0; k < sweeps; k++) {
+        for (int color = 0; color < 2; color++) {
+            const int last = color == 1;
+            if (precision == PCD_PREC_MIXED) {
+                if (track)
+                    k_rb_half<float, MASKED, true><<<blocks, kThreads, 0, s>>>(ws.e32, ws.r32, ws.mask, ws.ctl, a, color, last);
+                else
+                    k_rb_half<float, MASKED, false><<<blocks, kThreads, 0, s>>>(ws.e32, ws.r32, ws.mask, ws.ctl, a, color, last);
+            } else {
+                if (track)
+                    k_rb_half<double, MASKED, true><<<blocks, kThreads, 0, s>>>(phi, b, ws.mask, ws.ctl, a, color, last);
+                else
+                    k_rb_half<double, MASKED, false><<<blocks, kThreads, 0, s>>>(phi, b, ws.mask, ws.ctl, a, color, last);
+            }
+            n++;
+        }
+    }
+    if (precision == PCD_PREC_MIXED) {
+        k_refine_residual<MASKED><<<rblocks, kThreads, 0, s>>>(phi, ws.e32, b, ws.mask, ws.r32, ws.ctl, ws.partials, a, 0);
+        k_refine_update<<<rblocks, kThreads, 0, s>>>(phi, ws.e32, ws.ctl, a);
+        n += 2;
+    } else if (a.stop == PCD_STOP_REL_RESIDUAL) {
+        k_residual64<MASKED><<<rblocks, kThreads, 0, s>>>(phi, b, ws.mask, ws.ctl, ws.partials, a, 1, 0, 1);
+        n++;
+    }
+    PCD_CUDA(cudaGetLastError());
+    *nodes = n;
+    return PCD_OK;
+}
+
+int get_chunk_graph(SolverWorkspace &ws, const double *b, double *phi, const SolveArgs &a, int precision,
+                    int masked, int sweeps, cudaStream_t s, SolverWorkspace::GraphEntry **out)
+{
+    std::vector<long long> key = {(long long)(uintptr_t)b, (long long)(uintptr_t)phi, a.W, a.H, a.ld, a.stop,
+                                  a.max_iter, precision, masked, sweeps};
+    long long tb, ob;
+    std::memcpy(&tb, &a.tol, 8);
+    std::memcpy(&ob, &a.omega, 8);
+    key.push_back(tb);
+    key.push_back(ob);
+    auto it = ws.graphs.find(key);
+    if (it != ws.graphs.end()) {
+        *out = &it->second;
+        return PCD_OK;
+    }
+    cudaGraph_t g;
+    int nodes = 0;
+    PCD_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    int st = masked ? enqueue_chunk<true>(ws, b, phi, a, precision, sweeps, s, &nodes)
+                    : enqueue_chunk<false>(ws, b, phi, a, precision, sweeps, s, &nodes);
+    cudaError_t ce = cudaStreamEndCapture(s, &g);
+    if (st != PCD_OK) return st;
+    if (ce != cudaSuccess) {
+        set_error(std::string("cudaStreamEndCapture: ") + cudaGetErrorString(ce));
+        return PCD_DEVICE_ERROR;
+    }
+    cudaGraphExec_t exec;
+    ce = cudaGraphInstantiate(&exec, g, 0);
+    cudaGraphDestroy(g);
+    if (ce != cudaSuccess) {
+        set_error(std::string("cudaGraphInstantiate: ") + cudaGetErrorString(ce));
+        return PCD_DEVICE_ERROR;
+    }
+    if (ws.graphs.size() > 64) {
+        for (auto &kv : ws.graphs) cudaGraphExecDestroy(kv.second.exec);
+        ws.graphs.clear();
+    }
+    auto &e = ws.graphs[key];
+    e.exec = exec;
+    e.nodes = nodes;
+    *out = &e;
+    return PCD_OK;
+}
+
+}  // namespace
+
+namespace {
+
+// One cooperative launch per solve (sor_persist.cu), bracketed by the FP64
+// residual kernels that supply ||b|| / r64 before and the exact statistics after.
+int solve_persistent(SolverWorkspace &ws, const double *b, double *phi, const SolveArgs &a, int precision,
+                     const pcd_solve_opts &o, int G, size_t smem, pcd_solve_stats *stats, cudaStream_t s)
+{
+    const bool mixed = precision == PCD_PREC_MIXED;
+    const size_t xe = (size_t)G * 4 * a.W;
+    if (xe > ws.xbuf_elems) {
+        if (ws.xbuf) cudaFree(ws.xbuf);
+        ws.xbuf = nullptr;
+        ws.xbuf_elems = 0;
+        PCD_CUDA(cudaMalloc(&ws.xbuf, xe * sizeof(double)));
+        ws.xbuf_elems = xe;
+    }
+    if (G > ws.max_ctas) {
+        if (ws.flags) cudaFree(ws.flags);
+        if (ws.part) cudaFree(ws.part);
+        ws.flags = nullptr;
+        ws.part = nullptr;
+        ws.max_ctas = 0;
+        PCD_CUDA(cudaMalloc(&ws.flags, (G + 1) * sizeof(unsigned)));
+        PCD_CUDA(cudaMalloc(&ws.part, 2 * 3 * G * sizeof(double)));
+        ws.max_ctas = G;
+    }
+    PCD_CUDA(cudaMemsetAsync(ws.flags, 0, (G + 1) * sizeof(unsigned), s));
+
+    PersistArgs pa{};
+    pa.W = a.W; pa.H = a.H; pa.ld = a.ld; pa.G = G;
+    pa.b = b; pa.phi = phi; pa.r64 = ws.r64;
+    pa.xbuf = ws.xbuf; pa.flags = ws.flags; pa.bar = ws.flags + G; pa.part = ws.part; pa.ctl = ws.ctl;
+    pa.stop = a.stop; pa.max_iter = a.max_iter; pa.tol = a.tol;
+    if (o.check_every > 0) pa.check_every = o.check_every;
+    else if (a.stop == PCD_STOP_MAX_UPDATE) pa.check_every = mixed ? 16 : 8;
+    else pa.check_every = 32;
+    if (mixed && o.refine_every > 0 && o.refine_every < pa.check_every) pa.check_every = o.refine_every;
+    for (int c = 0; c < 5; c++) { pa.w64[c] = a.w64[c]; pa.w32[c] = a.w32[c]; }
+    pa.spin_limit = 1ll << 24;
+    PCD_CUDA(cudaEventRecord(ws.k0, s));
+    PCD_TRY(launch_persist(pa, mixed, smem, s));
+    PCD_CUDA(cudaEventRecord(ws.k1, s));
+
+    // exact FP64 statistics of the returned phi
+    const int rblocks = grid_blocks((long)a.W * a.H);
+    k_residual64<false><<<rblocks, kThreads, 0, s>>>(phi, b, ws.mask, ws.ctl, ws.partials, a, 0, 1, 0);
+    PCD_LAUNCHED(1);
+    PCD_CUDA(cudaEventRecord(ws.t1, s));
+    PCD_CUDA(cudaMemcpyAsync(&ws.ctl_host[0], ws.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, s));
+    PCD_CUDA(cudaStreamSynchronize(s));
+    const Ctl &c = ws.ctl_host[0];
+    if (c.error) {
+        set_error("persistent SOR: a bounded device wait gave up (status " + std::to_string(c.error) + ")");
+        return c.error;
+    }
+    int converged = c.converged;
+    if (a.stop == PCD_STOP_REL_RESIDUAL) converged = c.rel <= a.tol;
+    if (stats) {
+        stats->sweeps = c.sweeps;
+        stats->converged = converged;
+        stats->rel_residual = c.rel;
+        stats->max_residual = c.rmax;
+        stats->last_max_update = c.last_max;
+        stats->residual_checks = c.checks + 2;
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, ws.t0, ws.t1);
+        stats->device_ms = ms;
+        cudaEventElapsedTime(&ms, ws.k0, ws.k1);
+        stats->sweep_ms = ms;
+        stats->schedule_used = PCD_SCHED_PERSISTENT;
+    }
+    return converged ? PCD_OK : PCD_NOT_CONVERGED;
+}
+
+}  // namespace
+
+namespace {
+
+// Mixed precision on one cluster: cycles of [FP32 cluster sweeps, FP64
+// residual refresh, phi += e] until the FP64 relative residual passes.  The
+// next cycle is launched before the previous one's control block is read; a
+// cycle launched after convergence returns at once.
+int solve_cluster(SolverWorkspace &ws, const double *b, double *phi, const SolveArgs &a, const pcd_solve_opts &o,
+                  int C, size_t smem, pcd_solve_stats *stats, cudaStream_t s)
+{
+    const int rblocks = grid_blocks((long)a.W * a.H);
+    PCD_CUDA(cudaMemsetAsync(ws.e32, 0, sizeof(float) * (size_t)a.H * a.ld, s));
+    // r32 = b - L phi0; ||b||; stop test on the initial guess
+    k_refine_residual<false><<<rblocks, kThreads, 0, s>>>(phi, ws.e32, b, ws.mask, ws.r32, ws.ctl, ws.partials, a, 1);
+    PCD_LAUNCHED(1);
+    k_refine_update<<<rblocks, kThreads, 0, s>>>(phi, ws.e32, ws.ctl, a);
+    PCD_LAUNCHED(1);
+
+    ClusterArgs ca{};
+    ca.W = a.W; ca.H = a.H; ca.ld = a.ld;
+    ca.e = ws.e32; ca.r32 = ws.r32; ca.ctl = ws.ctl;
+    ca.check_every = o.check_every > 0 ? o.check_every : 16;
+    ca.cycle_cap = o.refine_every > 0 ? o.refine_every : 2048;
+    ca.max_iter = a.max_iter;
+    ca.tol = a.tol;
+    ca.drop = 3e-2;
+    for (int c = 0; c < 5; c++) ca.w32[c] = a.w32[c];
+
+    PCD_CUDA(cudaEventRecord(ws.k0, s));
+    long launched = 0;
+    const long max_cycles = (long)a.max_iter + 4;
+    bool finished = false;
+    while (!finished) {
+        if (launched >= max_cycles) {
+            set_error("cluster SOR: cycle budget exceeded without a done flag");
+            return PCD_TIMEOUT;
+        }
+        PCD_TRY(launch_cluster(ca, C, smem, s));
+        k_refine_residual<false><<<rblocks, kThreads, 0, s>>>(phi, ws.e32, b, ws.mask, ws.r32, ws.ctl, ws.partials, a, 0);
+        PCD_LAUNCHED(1);
+        k_refine_update<<<rblocks, kThreads, 0, s>>>(phi, ws.e32, ws.ctl, a);
+        PCD_LAUNCHED(1);
+        const int slot = (int)(launched & 1);
+        PCD_CUDA(cudaMemcpyAsync(&ws.ctl_host[slot], ws.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, s));
+        PCD_CUDA(cudaEventRecord(ws.ev[slot], s));
+        launched++;
+        if (launched >= 2) {
+            const int prev = (int)((launched - 2) & 1);
+            PCD_CUDA(cudaEventSynchronize(ws.ev[prev]));
+            if (ws.ctl_host[prev].done) finished = true;
+        }
+    }
+    PCD_CUDA(cudaEventRecord(ws.k1, s));
+    PCD_CUDA(cudaEventRecord(ws.t1, s));
+    PCD_CUDA(cudaMemcpyAsync(&ws.ctl_host[0], ws.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, s));
+    PCD_CUDA(cudaStreamSynchronize(s));
+    const Ctl &c = ws.ctl_host[0];
+    if (stats) {
+        stats->sweeps = c.sweeps;
+        stats->converged = c.converged;
+        stats->rel_residual = c.rel;
+        stats->max_residual = c.rmax;
+        stats->last_max_update = 0.0;
+        stats->residual_checks = c.checks;
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, ws.t0, ws.t1);
+        stats->device_ms = ms;
+        cudaEventElapsedTime(&ms, ws.k0, ws.k1);
+        stats->sweep_ms = ms;
+        stats->schedule_used = PCD_SCHED_CLUSTER;
+    }
+    return c.converged ? PCD_OK : PCD_NOT_CONVERGED;
+}
+
+}  // namespace
+
+int solve_device(SolverWorkspace &ws, const double *b, double *phi, int W, int H, int ld, const pcd_solve_opts &o,
+                 pcd_solve_stats *stats, cudaStream_t s)
+{
+    if (W < 1 || H < 1 || ld < W || !b || !phi) {
+        set_error("pcd solve: bad grid arguments");
+        return PCD_BAD_ARG;
+    }
+    if (o.max_iterations < 0 || o.stop < 0 || o.stop > 1 || o.precision < 0 || o.precision > 1) {
+        set_error("pcd solve: bad options");
+        return PCD_BAD_ARG;
+    }
+    PCD_TRY(ws.reserve((size_t)H * ld));
+
+    SolveArgs a;
+    a.W = W; a.H = H; a.ld = ld;
+    a.stop = o.stop;
+    a.max_iter = o.max_iterations;
+    a.tol = o.tol;
+    a.omega = resolve_omega(o.omega, W, H);
+    for (int c = 0; c < 5; c++) {
+        a.w64[c] = a.omega / (double)c;             // solver.cpp:47 divides omega by cnt
+        a.w32[c] = (float)a.omega / (float)c;
+    }
+    const int precision = o.precision;
+
+    PCD_CUDA(cudaEventRecord(ws.t0, s));
+    PCD_CUDA(cudaMemsetAsync(ws.ctl, 0, sizeof(Ctl), s));
+    const int rblocks = grid_blocks((long)W * H);
+    k_mask<<<rblocks, kThreads, 0, s>>>(b, ws.mask, W, H, ld, ws.ctl);
+    PCD_LAUNCHED(1);
+    if (!o.warm_start) {
+        k_fill<<<rblocks, kThreads, 0, s>>>(phi, W, H, ld, 0.0);
+        PCD_LAUNCHED(1);
+    }
+    // Initial FP64 residual (masked form: valid with or without NaN cells);
+    // it also yields ||b|| and, for the mixed form, the FP64 residual r64.
+    k_residual64<true><<<rblocks, kThreads, 0, s>>>(phi, b, ws.mask, ws.ctl, ws.partials, a,
+                                                   a.stop == PCD_STOP_REL_RESIDUAL, 1, 0,
+                                                   precision == PCD_PREC_MIXED ? ws.r64 : nullptr);
+    PCD_LAUNCHED(1);
+    PCD_CUDA(cudaMemcpyAsync(ws.ctl_host, ws.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, s));
+    PCD_CUDA(cudaStreamSynchronize(s));
+    const int masked = ws.ctl_host[0].nan_cells > 0 ? 1 : 0;
+    const bool done_already = ws.ctl_host[0].converged != 0 || a.max_iter == 0;
+
+    if (!done_already && !masked && precision == PCD_PREC_MIXED && a.stop == PCD_STOP_REL_RESIDUAL &&
+        (o.schedule == PCD_SCHED_AUTO || o.schedule == PCD_SCHED_CLUSTER)) {
+        int C = 0;
+        size_t smem = 0;
+        if (cluster_plan(ws.dev, W, H, &C, &smem) == PCD_OK)
+            return solve_cluster(ws, b, phi, a, o, C, smem, stats, s);
+    }
+    if (!done_already && !masked && o.schedule != PCD_SCHED_LAUNCHES) {
+        int G = 0;
+        size_t smem = 0;
+        if (persist_grid(ws.dev, W, H, precision == PCD_PREC_MIXED, &G, &smem) == PCD_OK)
+            return solve_persistent(ws, b, phi, a, precision, o, G, smem, stats, s);
+    }
+
+    if (done_already) {
+        int one = 1;
+        PCD_CUDA(cudaMemcpyAsync(&ws.ctl->halt, &one, sizeof(int), cudaMemcpyHostToDevice, s));
+        PCD_CUDA(cudaMemcpyAsync(&ws.ctl->done, &one, sizeof(int), cudaMemcpyHostToDevice, s));
+    } else if (precision == PCD_PREC_MIXED) {
+        // first right-hand side of the FP32 correction sweeps
+        PCD_CUDA(cudaMemsetAsync(ws.e32, 0, sizeof(float) * (size_t)H * ld, s));
+        if (masked)
+            k_refine_residual<true><<<rblocks, kThreads, 0, s>>>(phi, ws.e32, b, ws.mask, ws.r32, ws.ctl, ws.partials, a, 1);
+        else
+            k_refine_residual<false><<<rblocks, kThreads, 0, s>>>(phi, ws.e32, b, ws.mask, ws.r32, ws.ctl, ws.partials, a, 1);
+        PCD_LAUNCHED(1);
+    }
+
+    int chunk;
+    if (a.stop == PCD_STOP_MAX_UPDATE)
+        chunk = precision == PCD_PREC_MIXED ? (o.refine_every > 0 ? o.refine_every : 32) : 32;
+    else if (precision == PCD_PREC_MIXED)
+        chunk = o.refine_every > 0 ? o.refine_every : (o.check_every > 0 ? o.check_every : 32);
+    else
+        chunk = o.check_every > 0 ? o.check_every : 32;
+    if (chunk > a.max_iter && a.max_iter > 0) chunk = a.max_iter;
+
+    SolverWorkspace::GraphEntry *ge = nullptr;
+    if (!done_already) PCD_TRY(get_chunk_graph(ws, b, phi, a, precision, masked, chunk, s, &ge));
+
+    PCD_CUDA(cudaEventRecord(ws.k0, s));
+    // Chunk loop: launch chunk i+1 before inspecting chunk i's control block.
+    const long max_chunks = a.max_iter > 0 ? (long)a.max_iter / chunk + 3 : 0;
+    long launched = 0;
+    int finished = done_already;
+    auto flag_done = [&](const Ctl &c) { return precision == PCD_PREC_MIXED ? c.done : c.halt; };
+    while (!finished) {
+        if (launched >= max_chunks) {
+            set_error("pcd solve: chunk budget exceeded without a halt flag");
+            return PCD_TIMEOUT;
+        }
+        PCD_CUDA(cudaGraphLaunch(ge->exec, s));
+        count_launches(ge->nodes);
+        const int slot = (int)(launched & 1);
+        PCD_CUDA(cudaMemcpyAsync(&ws.ctl_host[slot], ws.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, s));
+        PCD_CUDA(cudaEventRecord(ws.ev[slot], s));
+        launched++;
+        if (launched >= 2) {
+            const int prev = (int)((launched - 2) & 1);
+            PCD_CUDA(cudaEventSynchronize(ws.ev[prev]));
+            if (flag_done(ws.ctl_host[prev])) finished = 1;
+        }
+    }
+    PCD_CUDA(cudaEventRecord(ws.k1, s));
+    // Final statistics (FP64 residual of the returned phi).
+    if (precision != PCD_PREC_MIXED) {
+        if (masked)
+            k_residual64<true><<<rblocks, kThreads, 0, s>>>(phi, b, ws.mask, ws.ctl, ws.partials, a, 0, 1, 0);
+        else
+            k_residual64<false><<<rblocks, kThreads, 0, s>>>(phi, b, ws.mask, ws.ctl, ws.partials, a, 0, 1, 0);
+        PCD_LAUNCHED(1);
+    }
+    PCD_CUDA(cudaEventRecord(ws.t1, s));
+    PCD_CUDA(cudaMemcpyAsync(&ws.ctl_host[0], ws.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, s));
+    PCD_CUDA(cudaStreamSynchronize(s));
+    const Ctl &c = ws.ctl_host[0];
+    if (stats) {
+        stats->sweeps = c.sweeps;
+        stats->converged = c.converged;
+        stats->rel_residual = c.rel;
+        stats->max_residual = c.rmax;
+        stats->last_max_update = c.last_max;
+        stats->residual_checks = c.checks;
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, ws.t0, ws.t1);
+        stats->device_ms = ms;
+        cudaEventElapsedTime(&ms, ws.k0, ws.k1);
+        stats->sweep_ms = ms;
+        stats->schedule_used = PCD_SCHED_LAUNCHES;
+    }
+    return c.converged ? PCD_OK : PCD_NOT_CONVERGED;
+}
+
+}  // namespace pcd

@@ -1,0 +1,86 @@
+// solver.cuh -- red-black SOR Poisson solver of libpcd_gb300 (internal).
+//
+// Solves  sum_nbr phi - cnt*phi = b  (the Neumann graph Laplacian of the
+// reference, src/solver.cpp:29-47) on a W x H grid with leading dimension ld.
+// A neighbour counts when it lies inside the grid and its b is not NaN.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <map>
+#include <tuple>
+#include <vector>
+
+#include "common.cuh"
+
+namespace pcd {
+
+// Device-resident control block of one solve.  Flags are written only by the
+// last block of a kernel (after every block of that kernel has finished) and
+// read by later kernels, so no kernel races with its own writes.
+struct Ctl {
+    int halt;                    // no further sweeps
+    int done;                    // solve finished (mixed: last correction folded in)
+    int converged;               // stop test passed
+    int sweeps;                  // full red+black sweeps done
+    unsigned int blocks_done;    // last-block counter of the sweep kernels
+    unsigned int blocks_done_r;  // last-block counter of the residual kernels
+    int checks;                  // residual evaluations
+    int nan_cells;               // NaN entries of b
+    int error;                   // PCD_TIMEOUT when a bounded device wait gave up
+    int pad_;
+    unsigned long long maxbits;  // running max |delta| of the current sweep
+    double last_max;             // max |delta| of the last full sweep
+    double rnorm, bnorm, rmax, rel;
+};
+
+struct SolveArgs {
+    int W, H, ld;
+    int stop;         // pcd_stop
+    int max_iter;
+    double tol;
+    double omega;
+    double w64[5];   // omega / cnt for cnt = 0..4, divided once on the host
+    float w32[5];    // the same in FP32 ((float)omega / cnt)
+};
+
+// omega > 0: used as given; omega == 0: the reference's 2/(1+pi/width)
+// (solver.cpp:71); omega < 0: 2/(1+sin t) with cos t = (1+cos(pi/n))/2,
+// n = max(width, height), the optimum for the Neumann operator (its slowest
+// mode varies along one axis only, so the reference's value is too small).
+double resolve_omega(double omega, int W, int H);
+
+// Per-context workspace of the solver; grows on demand.
+struct SolverWorkspace {
+    int dev = 0;
+    size_t cells = 0;           // capacity in elements of the per-cell buffers
+    uint8_t *mask = nullptr;    // neighbour-validity bits per cell
+    float *e32 = nullptr;       // FP32 correction (mixed precision)
+    float *r32 = nullptr;       // FP32 right-hand side of the correction equation
+    double *partials = nullptr; // per-block reduction partials
+    int max_partials = 0;
+    Ctl *ctl = nullptr;         // device control block
+    Ctl *ctl_host = nullptr;    // pinned copies, 2 slots
+    cudaEvent_t ev[2] = {nullptr, nullptr};
+    cudaEvent_t t0 = nullptr, t1 = nullptr, k0 = nullptr, k1 = nullptr;
+    // persistent-kernel state
+    double *r64 = nullptr;      // FP64 residual (mixed form)
+    double *xbuf = nullptr;     // exchange rows
+    size_t xbuf_elems = 0;
+    unsigned *flags = nullptr;  // epoch flags + barrier counter
+    int max_ctas = 0;
+    double *part = nullptr;     // check partials
+
+    struct GraphEntry {
+        cudaGraphExec_t exec;
+        int nodes;
+    };
+    std::map<std::vector<long long>, GraphEntry> graphs;
+
+    int reserve(size_t n);
+    void release();
+};
+
+int solve_device(SolverWorkspace &ws, const double *b, double *phi, int W, int H, int ld,
+                 const pcd_solve_opts &o, pcd_solve_stats *stats, cudaStream_t s);
+
+}  // namespace pcd

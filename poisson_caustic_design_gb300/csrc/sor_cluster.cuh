@@ -1,0 +1,28 @@
+// sor_cluster.cuh -- FP32 red-black SOR on one thread-block cluster (internal).
+#pragma once
+
+#include "solver.cuh"
+
+namespace pcd {
+
+constexpr int kClusterThreads = 1024;
+
+struct ClusterArgs {
+    int W, H, ld;
+    float *e;            // FP32 correction (global, ld-strided), in/out
+    const float *r32;    // FP32 right-hand side
+    Ctl *ctl;            // reads bnorm / rnorm / sweeps, writes sweeps / halt
+    int check_every;     // sweeps between FP32 residual estimates
+    int cycle_cap;       // sweeps per cycle at most
+    int max_iter;        // total sweep cap
+    double tol;          // relative stop tolerance
+    double drop;         // end the cycle when the estimate fell by this factor
+    float w32[5];        // omega / cnt
+};
+
+// Cluster size (16 or 8 CTAs) and dynamic shared memory for a W x H grid;
+// PCD_BAD_ARG when the grid does not fit in one cluster.
+int cluster_plan(int dev, int W, int H, int *C_out, size_t *smem_out);
+int launch_cluster(ClusterArgs &a, int C, size_t smem, cudaStream_t s);
+
+}  // namespace pcd

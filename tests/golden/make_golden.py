@@ -54,9 +54,11 @@ def solver_cases(R: O.Ref):
     b = inputs.poisson_rhs(48, 4, "gaussian", m=40)
     b[10:14, 20:27] = np.nan
     b[0, 0] = np.nan
+    b = R.subtract_average(b)   # consistent again on the non-NaN cells (utils.cpp:60-86)
     add("nanhole_48x40", b, np.zeros_like(b), 100000, 1e-8)
     add("capped_64", inputs.poisson_rhs(64, 5, "binary"), np.zeros((64, 64)), 50, 1e-12)
-    add("single_row_16x1", rng.standard_normal((1, 16)) - 0.0, np.zeros((1, 16)), 300, 1e-9)
+    b = rng.standard_normal((1, 16)); b -= b.mean()
+    add("single_row_16x1", b, np.zeros((1, 16)), 3000, 1e-9)
     np.savez_compressed(os.path.join(OUT, "solver_cases.npz"), **cases)
 
 

@@ -1,0 +1,55 @@
+"""The reference's C++ signatures (include/pcd_legacy.hpp) over the C ABI:
+a program written like the reference's main.cpp compiles against the header,
+links libpcd_gb300.so and reproduces the reference pipeline."""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+from conftest import ROOT, load_golden
+
+SRC = os.path.join(ROOT, "tests", "cpp", "shim_main.cpp")
+INC = os.path.join(ROOT, "include")
+
+
+def test_shim_compiles_cpu():
+    r = subprocess.run(["g++", "-std=c++17", "-fsyntax-only", "-Wall", "-I" + INC, SRC], capture_output=True,
+                       text=True)
+    assert r.returncode == 0, r.stderr
+
+
+def test_c_header_is_plain_c():
+    hdr = os.path.join(INC, "pcd.h")
+    r = subprocess.run(["gcc", "-std=c99", "-fsyntax-only", "-Wall", "-x", "c", hdr], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+
+
+@pytest.mark.gpu
+def test_shim_pipeline_matches_reference(tmp_path):
+    import oracle
+    from poisson_caustic_design_gb300 import _lib, build
+
+    _lib.load()
+    exe = tmp_path / "shim_main"
+    libdir = os.path.dirname(build.LIB)
+    r = subprocess.run(["g++", "-std=c++17", "-O2", "-I" + INC, SRC, "-o", str(exe), "-L" + libdir, "-lpcd_gb300",
+                        "-Wl,-rpath," + libdir], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    z = load_golden("pipeline_r16.npz")
+    img = tmp_path / "img.f64"
+    out = tmp_path / "out.f64"
+    np.ascontiguousarray(z["image"], dtype=np.float64).tofile(img)
+    r = subprocess.run([str(exe), "16", str(img), str(out)], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, (r.returncode, r.stdout, r.stderr)
+    v = np.fromfile(out)
+    n = 16 * 16
+    steps = v[:50]
+    steps = steps[~np.isnan(steps)]
+    tp = v[50:50 + 3 * n].reshape(n, 3)
+    sp = v[50 + 3 * n:50 + 6 * n].reshape(n, 3)
+    h = v[50 + 6 * n:].reshape(64, 64)
+    np.testing.assert_allclose(steps, z["steps"], rtol=1e-5)
+    assert np.linalg.norm(tp - z["target_points"]) / np.linalg.norm(z["target_points"]) < 1e-5
+    assert np.linalg.norm(sp[:, 2] - z["source_points"][:, 2]) / np.linalg.norm(z["source_points"][:, 2]) < 1e-5
+    assert oracle.rel_err_mod_const(h, z["h"])[0] < 1e-4

@@ -1,0 +1,115 @@
+"""Parity of the GPU caustic-design iterations with the reference pipeline.
+
+Golden fixtures come from the reference's own Caustic_design (compiled
+sources, max_threads=1) replaying main.cpp:216-262; the C port (oracle) is
+run beside it for per-step checks.  Tolerances: 1e-5 relative L2 for the
+final vertex positions and heights (FP64 plain form), per-step fields to
+rounding-level bounds stated inline.
+"""
+import numpy as np
+import pytest
+
+from conftest import load_golden
+
+pytestmark = pytest.mark.gpu
+
+
+def _design(ctx, z):
+    import poisson_caustic_design_gb300 as pcd
+
+    r, width, focal, thickness, conv, seed = z["params"]
+    r = int(r)
+    d = pcd.CausticDesign(ctx)
+    d.set_mesh_resolution(r, r)
+    d.set_domain_resolution(4 * r, 4 * r)
+    d.set_mesh_size(width, width)
+    d.set_lens_focal_length(focal)
+    d.set_lens_thickness(thickness)
+    d.set_solver_max_threads(1)
+    d.initialize_solvers(z["image"])
+    return d, conv
+
+
+def _rel(a, b):
+    return float(np.linalg.norm(np.asarray(a) - np.asarray(b)) / np.linalg.norm(b))
+
+
+@pytest.mark.parametrize("res", [16, 32, 64])
+def test_full_pipeline_matches_reference(ctx, res):
+    import oracle
+
+    z = load_golden(f"pipeline_r{res}.npz")
+    d, conv = _design(ctx, z)
+    np.testing.assert_allclose(d.target_areas, z["target_areas"], rtol=1e-10, atol=1e-16)
+    steps = []
+    for itr in range(50):
+        s = d.perform_transport_iteration()
+        if itr == 0:
+            assert _rel(d.errors, z["errors_0"]) < 1e-9
+            assert np.abs(d.raster - z["raster_0"]).max() < 1e-9 * np.abs(z["raster_0"]).max()
+            assert oracle.rel_err_mod_const(d.phi, z["phi_0"])[0] < 1e-5
+        steps.append(s)
+        if s < conv:
+            break
+    assert len(steps) == len(z["steps"])
+    np.testing.assert_allclose(steps, z["steps"], rtol=1e-5)
+    tp = d.target_points()
+    assert _rel(tp, z["target_points"]) < 1e-5
+    assert np.abs(tp - z["target_points"]).max() < 1e-6
+    assert oracle.rel_err_mod_const(d.phi, z["phi"])[0] < 1e-5
+    for itr in range(3):
+        d.perform_height_map_iteration(itr)
+        if itr == 0:
+            assert _rel(d.normals[0], z["normals_x_0"]) < 1e-6
+            assert _rel(d.normals[1], z["normals_y_0"]) < 1e-6
+            assert _rel(d.divergence, z["divergence_0"]) < 1e-6
+    sp = d.source_points()
+    assert _rel(sp[:, 2], z["source_points"][:, 2]) < 1e-5
+    # The reference's own h is only within 1.6e-5..3.5e-5 of the exact solve of
+    # its final right-hand side (its height solve stops on max|delta| < 1e-8 at
+    # |h| ~ 0.03; tests/test_oracle.py pins this), so the h grid is compared
+    # at 1e-4; the vertex heights above meet 1e-5.
+    assert oracle.rel_err_mod_const(d.h, z["h"])[0] < 1e-4
+    np.testing.assert_array_equal(sp[:, :2], z["source_points"][:, :2])
+    d.close()
+
+
+def test_step_kernels_match_port_bitwise_where_defined(ctx, port):
+    """Given the same phi, the vertex step of the GPU equals the port's to
+    rounding: run one GPU transport iteration and replay its sampling/step on
+    the CPU from the GPU's own phi."""
+    import oracle
+
+    z = load_golden("pipeline_r16.npz")
+    d, _ = _design(ctx, z)
+    tp0 = d.target_points()
+    s = d.perform_transport_iteration()
+    phi = d.phi
+    gx, gy = port.gradient(phi)
+    W = H = 0.5
+    vgx = port.sample_vertices(gx, tp0, W, H)
+    vgy = port.sample_vertices(gy, tp0, W, H)
+    np.testing.assert_allclose(d.vertex_gradient[0], vgx, rtol=0, atol=1e-13 * np.abs(vgx).max())
+    np.testing.assert_allclose(d.vertex_gradient[1], vgy, rtol=0, atol=1e-13 * np.abs(vgy).max())
+    tp = tp0.copy()
+    s_cpu = port.step_grid(tp, vgx, vgy, 16, 16, W, float(np.float32(0.05)))
+    assert abs(s - s_cpu) < 1e-12 * s_cpu
+    assert np.abs(d.target_points() - tp).max() < 1e-15
+    d.close()
+
+
+def test_raster_matches_port_on_deformed_mesh(ctx, port):
+    """The GPU rasteriser (lowest-index owner) reproduces the port's raster of
+    the same errors on the deformed mesh."""
+    z = load_golden("pipeline_r32.npz")
+    d, _ = _design(ctx, z)
+    for _ in range(3):
+        d.perform_transport_iteration()
+    tp = d.target_points()
+    d.perform_transport_iteration()   # its raster is built on tp
+    errs = d.errors
+    ras_cpu, miss = port.raster(tp, errs, 32, 32, 0.5, 0.5, 128, 128)
+    assert miss == 0
+    ras_cpu = port.subtract_average(ras_cpu)
+    assert np.abs(d.raster - ras_cpu).max() < 1e-12 * np.abs(ras_cpu).max()
+    d.close()
