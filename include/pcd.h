@@ -139,6 +139,20 @@ int pcd_gradient_device(pcd_ctx *ctx, const double *g, double *gx, double *gy, i
 int pcd_divergence_device(pcd_ctx *ctx, const double *nx, const double *ny, double *div,
                           int width, int height, void *stream);
 
+/* Mean removal that allocates no device memory (no counterpart in the
+ * reference; it is an extra entry point of this library).  For callers that
+ * cannot let a library call cudaMalloc -- a host application that gives its
+ * whole device-memory budget to its own pool, or a latency-critical path where
+ * an allocation would synchronise the device.  Same result as
+ * pcd_subtract_average_device on g (device array, width*height, dense), on the
+ * CURRENT device, enqueued on `stream` (NULL = legacy default stream).  Its
+ * scratch is a static device array of 2*16384+2 doubles held by every GPU
+ * that loads the library until exit, so height must be <= 16384 (else
+ * PCD_BAD_ARG).  The first call on a device looks up that array's device
+ * address (make it before any stream capture).  All calls share the array:
+ * calls that overlap on the GPU race and must be serialised by the caller. */
+int pcd_subtract_average_noalloc(double *g, int width, int height, void *stream);
+
 /* ---- Caustic_design ----------------------------------------------------- */
 typedef enum {
     PCD_GRID_PHI = 0, PCD_GRID_H = 1, PCD_GRID_RASTER = 2, PCD_GRID_DIVERGENCE = 3,

@@ -105,6 +105,7 @@ SIGNATURES = {
     "pcd_subtract_average_device": (C.c_int, [_vp, _vp, C.c_int, C.c_int, _vp]),
     "pcd_gradient_device": (C.c_int, [_vp, _vp, _vp, _vp, C.c_int, C.c_int, _vp]),
     "pcd_divergence_device": (C.c_int, [_vp, _vp, _vp, _vp, C.c_int, C.c_int, _vp]),
+    "pcd_subtract_average_noalloc": (C.c_int, [_vp, C.c_int, C.c_int, _vp]),
     "pcd_design_params_default": (C.c_int, [C.POINTER(DesignParams)]),
     "pcd_design_create": (C.c_int, [_vp, C.POINTER(DesignParams), C.POINTER(_vp)]),
     "pcd_design_destroy": (C.c_int, [_vp]),
