@@ -555,7 +555,7 @@ namespace {
 // next cycle is launched before the previous one's control block is read; a
 // cycle launched after convergence returns at once.
 int solve_cluster(SolverWorkspace &ws, const double *b, double *phi, const SolveArgs &a, const pcd_solve_opts &o,
-                  int C, size_t smem, pcd_solve_stats *stats, cudaStream_t s)
+                  int C, size_t smem, int khp, pcd_solve_stats *stats, cudaStream_t s)
 {
     const int rblocks = grid_blocks((long)a.W * a.H);
     PCD_CUDA(cudaMemsetAsync(ws.e32, 0, sizeof(float) * (size_t)a.H * a.ld, s));
@@ -566,7 +566,7 @@ int solve_cluster(SolverWorkspace &ws, const double *b, double *phi, const Solve
     PCD_LAUNCHED(1);
 
     ClusterArgs ca{};
-    ca.W = a.W; ca.H = a.H; ca.ld = a.ld;
+    ca.W = a.W; ca.H = a.H; ca.ld = a.ld; ca.khp = khp;
     ca.e = ws.e32; ca.r32 = ws.r32; ca.ctl = ws.ctl;
     ca.check_every = o.check_every > 0 ? o.check_every : 16;
     ca.cycle_cap = o.refine_every > 0 ? o.refine_every : 2048;
@@ -670,10 +670,10 @@ int solve_device(SolverWorkspace &ws, const double *b, double *phi, int W, int H
 
     if (!done_already && !masked && precision == PCD_PREC_MIXED && a.stop == PCD_STOP_REL_RESIDUAL &&
         (o.schedule == PCD_SCHED_AUTO || o.schedule == PCD_SCHED_CLUSTER)) {
-        int C = 0;
+        int C = 0, khp = 0;
         size_t smem = 0;
-        if (cluster_plan(ws.dev, W, H, &C, &smem) == PCD_OK)
-            return solve_cluster(ws, b, phi, a, o, C, smem, stats, s);
+        if (cluster_plan(ws.dev, W, H, &C, &smem, &khp) == PCD_OK)
+            return solve_cluster(ws, b, phi, a, o, C, smem, khp, stats, s);
     }
     if (!done_already && !masked && o.schedule != PCD_SCHED_LAUNCHES) {
         int G = 0;

@@ -9,6 +9,7 @@ constexpr int kClusterThreads = 1024;
 
 struct ClusterArgs {
     int W, H, ld;
+    int khp;             // shared-memory row stride of a colour plane (multiple of 4)
     float *e;            // FP32 correction (global, ld-strided), in/out
     const float *r32;    // FP32 right-hand side
     Ctl *ctl;            // reads bnorm / rnorm / sweeps, writes sweeps / halt
@@ -22,7 +23,7 @@ struct ClusterArgs {
 
 // Cluster size (16 or 8 CTAs) and dynamic shared memory for a W x H grid;
 // PCD_BAD_ARG when the grid does not fit in one cluster.
-int cluster_plan(int dev, int W, int H, int *C_out, size_t *smem_out);
+int cluster_plan(int dev, int W, int H, int *C_out, size_t *smem_out, int *khp_out);
 int launch_cluster(ClusterArgs &a, int C, size_t smem, cudaStream_t s);
 
 }  // namespace pcd
