@@ -80,9 +80,12 @@ typedef enum {
     PCD_SCHED_LAUNCHES = 1,    /* one kernel per half sweep, CUDA-graph chunks (any grid) */
     PCD_SCHED_PERSISTENT = 2,  /* one cooperative launch per solve, bands in shared memory
                                   (no NaN cells, band fits on chip) */
-    PCD_SCHED_CLUSTER = 3      /* mixed precision with the relative-residual stop: FP32 sweeps
+    PCD_SCHED_CLUSTER = 3,     /* mixed precision with the relative-residual stop: FP32 sweeps
                                   on one 16-CTA cluster (grid fits in its shared memory),
                                   FP64 defect correction on all SMs between cycles */
+    PCD_SCHED_STRIPES = 4      /* grids in HBM without NaN cells: one fused red+black pass per
+                                  sweep (row stripes walked top-down), CUDA-graph chunks; AUTO
+                                  picks it when the on-chip schedules do not fit */
 } pcd_schedule;
 
 typedef struct {
@@ -131,6 +134,37 @@ int pcd_poisson_solve(pcd_ctx *ctx, const double *b, double *phi, int width, int
 int pcd_poisson_solve_device(pcd_ctx *ctx, const double *b, double *phi, int width, int height,
                              int ld, const pcd_solve_opts *opts, pcd_solve_stats *stats,
                              void *stream);
+
+/* ---- batched solve (no counterpart in the reference: it solves one grid per
+ * call; this runs many independent grids of uneven sizes in one persistent
+ * launch, captured in a CUDA graph) ------------------------------------- */
+typedef struct {
+    int width, height, ld;   /* ld >= width; 32 <= height, width <= 4096 */
+    const double *b;         /* device, right-hand side */
+    double *phi;             /* device, solution (warm start when opts->warm_start) */
+} pcd_instance;
+
+typedef struct {
+    int sweeps;
+    int converged;
+    double rel_residual;     /* FP64 ||b - L phi|| / ||b|| at exit */
+    int cycles;              /* FP64 defect-correction cycles */
+} pcd_instance_stats;
+
+typedef struct {
+    double device_ms;        /* the graph launch, CUDA events */
+    int clusters;            /* co-resident clusters used */
+    int cluster_size;        /* CTAs per cluster (one per SM) */
+    long long smem_bytes;    /* dynamic shared memory per CTA */
+    long long cell_sweeps;   /* sum over instances of width*height*sweeps */
+} pcd_batch_stats;
+
+/* Mixed precision (FP32 sweeps, FP64 defect correction) with the relative-
+ * residual stop; opts->omega as in pcd_solve_opts, per instance.  Each 16-CTA
+ * cluster takes instances from a work queue (largest first) and solves them
+ * whole.  stats has `count` entries in the caller's order. */
+int pcd_batch_solve_device(pcd_ctx *ctx, const pcd_instance *inst, int count, const pcd_solve_opts *opts,
+                           pcd_instance_stats *stats, pcd_batch_stats *batch_stats, void *stream);
 
 /* ---- grid utilities on device arrays (dense, ld == width) -------------- */
 int pcd_subtract_average_device(pcd_ctx *ctx, double *g, int width, int height, void *stream);

@@ -32,6 +32,7 @@ SCHED_AUTO = 0
 SCHED_LAUNCHES = 1
 SCHED_PERSISTENT = 2
 SCHED_CLUSTER = 3
+SCHED_STRIPES = 4
 
 
 class PCDError(RuntimeError):
@@ -86,6 +87,19 @@ class DesignParams(C.Structure):
     ]
 
 
+class Instance(C.Structure):
+    _fields_ = [("width", C.c_int), ("height", C.c_int), ("ld", C.c_int), ("b", C.c_void_p), ("phi", C.c_void_p)]
+
+
+class InstanceStats(C.Structure):
+    _fields_ = [("sweeps", C.c_int), ("converged", C.c_int), ("rel_residual", C.c_double), ("cycles", C.c_int)]
+
+
+class BatchStats(C.Structure):
+    _fields_ = [("device_ms", C.c_double), ("clusters", C.c_int), ("cluster_size", C.c_int),
+                ("smem_bytes", C.c_longlong), ("cell_sweeps", C.c_longlong)]
+
+
 _vp = C.c_void_p
 _dp = C.POINTER(C.c_double)
 
@@ -103,6 +117,8 @@ SIGNATURES = {
     "pcd_poisson_solve_device": (C.c_int, [_vp, _vp, _vp, C.c_int, C.c_int, C.c_int, C.POINTER(SolveOpts),
                                            C.POINTER(SolveStats), _vp]),
     "pcd_subtract_average_device": (C.c_int, [_vp, _vp, C.c_int, C.c_int, _vp]),
+    "pcd_batch_solve_device": (C.c_int, [_vp, C.POINTER(Instance), C.c_int, C.POINTER(SolveOpts),
+                                         C.POINTER(InstanceStats), C.POINTER(BatchStats), _vp]),
     "pcd_gradient_device": (C.c_int, [_vp, _vp, _vp, _vp, C.c_int, C.c_int, _vp]),
     "pcd_divergence_device": (C.c_int, [_vp, _vp, _vp, _vp, C.c_int, C.c_int, _vp]),
     "pcd_subtract_average_noalloc": (C.c_int, [_vp, C.c_int, C.c_int, _vp]),

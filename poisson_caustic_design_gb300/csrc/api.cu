@@ -121,6 +121,7 @@ int pcd_ctx_destroy(pcd_ctx *ctx)
     design_detach_all(ctx);
     ctx->solver.release();
     ctx->grid.release();
+    ctx->batch.release();
     if (ctx->d_b) cudaFree(ctx->d_b);
     if (ctx->d_phi) cudaFree(ctx->d_phi);
     cudaStreamDestroy(ctx->stream);
@@ -200,6 +201,23 @@ int pcd_poisson_solver(const double *D, double *phi, int width, int height, int 
     o.precision = PCD_PREC_FP64;
     o.warm_start = 1;
     return pcd_poisson_solve(ctx, D, phi, width, height, &o, nullptr);
+}
+
+int pcd_batch_solve_device(pcd_ctx *ctx, const pcd_instance *inst, int count, const pcd_solve_opts *opts,
+                           pcd_instance_stats *stats, pcd_batch_stats *batch_stats, void *stream)
+{
+    if (!ctx) return PCD_BAD_ARG;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    PCD_TRY(ctx_activate(ctx));
+    pcd_solve_opts o;
+    if (opts) o = *opts;
+    else {
+        pcd_solve_opts_default(&o);
+        o.stop = PCD_STOP_REL_RESIDUAL;
+        o.tol = 1e-6;
+    }
+    return batch_solve_device(ctx->batch, ctx->device, inst, count, o, stats, batch_stats,
+                              stream ? (cudaStream_t)stream : ctx->stream);
 }
 
 int pcd_subtract_average_device(pcd_ctx *ctx, double *g, int width, int height, void *stream)

@@ -7,12 +7,14 @@
 #include "common.cuh"
 #include "grid.cuh"
 #include "solver.cuh"
+#include "sor_batch.cuh"
 
 struct pcd_ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
     pcd::SolverWorkspace solver;
     pcd::GridScratch grid;
+    pcd::BatchWorkspace batch;
     // device staging of the host-array entry points
     double *d_b = nullptr;
     double *d_phi = nullptr;

@@ -305,6 +305,139 @@ __global__ void __launch_bounds__(kThreads)
     }
 }
 
+
+// ---------------------------------------------------------------------------
+// Fused red+black sweep for grids that live in HBM (no NaN cells).
+//
+// Block s walks down its stripe of rows [y0, y1): at step j it relaxes the red
+// cells of row y0+j and then the black cells of row y0+j-1.  A red cell needs
+// the black rows y-1, y, y+1 as they were before the sweep, and a black cell
+// needs the new red rows y-1, y, y+1; walking down the stripe gives exactly
+// that order, with one block barrier per step.  The black cells of the first
+// and last row of every stripe depend on a neighbouring stripe's red row, so a
+// second kernel relaxes those after all stripes finished.  The result is
+// exactly one red-black SOR sweep, and phi and b cross HBM once per sweep
+// (24 B per cell in FP64, 12 B in FP32) instead of twice.
+constexpr int kStripeThreads = 512;
+
+__device__ __forceinline__ void prefetch_l2(const void *p)
+{
+    asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
+}
+
+// One colour of row y.  All loads of a thread's cells are issued before any
+// store: a cell's neighbours have the other colour, so no cell of this row
+// reads what another cell of it writes, and batching lets the DRAM latency of
+// the cells overlap instead of serialising behind each store.
+constexpr int kRowCellsMax = 8;  // cells per thread per row: W <= 2 * 8 * kStripeThreads
+
+template <typename T, bool TRACK, int CELLS>
+__device__ __forceinline__ double relax_row(T *__restrict__ phi, const T *__restrict__ rhs, const SolveArgs &a,
+                                            int y, int color)
+{
+    const int W = a.W, H = a.H, ld = a.ld;
+    const int off = (y + color) & 1;
+    const long rowi = (long)y * ld;
+    T sum[CELLS], v[CELLS], r[CELLS];
+    int cnt[CELLS];
+#pragma unroll
+    for (int j = 0; j < CELLS; j++) {
+        const int x = 2 * (threadIdx.x + j * (int)blockDim.x) + off;
+        sum[j] = T(0);
+        cnt[j] = 0;
+        v[j] = T(0);
+        r[j] = T(0);
+        if (x < W) {
+            const long i = rowi + x;
+            if (x > 0) { sum[j] += phi[i - 1]; cnt[j]++; }
+            if (y > 0) { sum[j] += phi[i - ld]; cnt[j]++; }
+            if (x < W - 1) { sum[j] += phi[i + 1]; cnt[j]++; }
+            if (y < H - 1) { sum[j] += phi[i + ld]; cnt[j]++; }
+            v[j] = phi[i];
+            r[j] = rhs[i];
+        }
+    }
+    double m = 0.0;
+#pragma unroll
+    for (int j = 0; j < CELLS; j++) {
+        const int x = 2 * (threadIdx.x + j * (int)blockDim.x) + off;
+        if (x < W) {
+            const T delta = omega_over_cnt<T>(a, cnt[j]) * (sum[j] - (T)cnt[j] * v[j] - r[j]);
+            phi[rowi + x] = v[j] + delta;
+            if (TRACK) {
+                const double ad = fabs((double)delta);
+                m = ad > m ? ad : m;
+            }
+        }
+    }
+    return m;
+}
+
+template <typename T, bool TRACK, int CELLS>
+__global__ void __launch_bounds__(kStripeThreads, 2)
+    k_stripe_a(T *__restrict__ phi, const T *__restrict__ rhs, Ctl *ctl, SolveArgs a, int R)
+{
+    if (vol_load(&ctl->halt)) return;
+    const int y0 = blockIdx.x * R, y1 = min(y0 + R, a.H);
+    double m = 0.0;
+    // lines of one row (128 B each); threads [0, L) prefetch the next step's
+    // new phi row, threads [L, 2L) its right-hand-side row
+    const int L = (int)((a.W * sizeof(T) + 127) / 128);
+    for (int j = 0; j <= y1 - y0; j++) {
+        const int yr = y0 + j;
+        const int t = threadIdx.x;
+        if (yr + 2 < a.H && t < L) prefetch_l2(phi + (long)(yr + 2) * a.ld + t * (128 / sizeof(T)));
+        else if (yr + 1 < y1 && t >= L && t < 2 * L)
+            prefetch_l2(rhs + (long)(yr + 1) * a.ld + (t - L) * (128 / sizeof(T)));
+        if (yr < y1) m = fmax(m, relax_row<T, TRACK, CELLS>(phi, rhs, a, yr, 0));
+        __syncthreads();
+        const int yb = yr - 1;
+        if (yb >= y0 + 1 && yb <= y1 - 2) m = fmax(m, relax_row<T, TRACK, CELLS>(phi, rhs, a, yb, 1));
+    }
+    if (TRACK) {
+        double v[1] = {m};
+        block_reduce<1, 1u>(v);
+        if (threadIdx.x == 0 && v[0] > 0.0) atomicMax(&ctl->maxbits, (unsigned long long)__double_as_longlong(v[0]));
+    }
+}
+
+// Black cells of the first and last row of every stripe; the last block
+// closes the sweep (end_of_sweep).  blockIdx.y = 2*stripe + {0: first, 1: last}.
+template <typename T, bool TRACK, int CELLS>
+__global__ void __launch_bounds__(kStripeThreads, 2)
+    k_stripe_b(T *__restrict__ phi, const T *__restrict__ rhs, Ctl *ctl, SolveArgs a, int R)
+{
+    if (vol_load(&ctl->halt)) return;
+    const int st = blockIdx.y >> 1, which = blockIdx.y & 1;
+    const int y0 = st * R, y1 = min(y0 + R, a.H);
+    const int y = which ? y1 - 1 : y0;
+    double m = 0.0;
+    if (!(which && y == y0)) m = relax_row<T, TRACK, CELLS>(phi, rhs, a, y, 1);
+    if (TRACK) {
+        double v[1] = {m};
+        block_reduce<1, 1u>(v);
+        m = v[0];
+    }
+    if (threadIdx.x == 0) {
+        if (TRACK && m > 0.0) atomicMax(&ctl->maxbits, (unsigned long long)__double_as_longlong(m));
+        __threadfence();
+        const unsigned t = atomicAdd(&ctl->blocks_done, 1u);
+        if (t == gridDim.x * gridDim.y - 1) {
+            __threadfence();
+            end_of_sweep(ctl, a);
+        }
+    }
+}
+
+// Rows per stripe such that all stripes are resident at once (one wave):
+// stripes = resident blocks per SM x SMs.
+inline int stripe_rows(int H, int resident)
+{
+    const int target = resident > 0 ? resident : 304;
+    int R = (H + target - 1) / target;
+    return R < 3 ? 3 : R;
+}
+
 __global__ void k_fill(double *p, int W, int H, int ld, double v)
 {
     const long n = (long)W * H;
@@ -386,16 +519,51 @@ void SolverWorkspace::release()
 
 namespace {
 
+template <typename T, bool TRACK, int CELLS>
+void launch_stripes_c(T *phi, const T *rhs, Ctl *ctl, const SolveArgs &a, int R, int ns, dim3 gb, cudaStream_t s)
+{
+    k_stripe_a<T, TRACK, CELLS><<<ns, kStripeThreads, 0, s>>>(phi, rhs, ctl, a, R);
+    k_stripe_b<T, TRACK, CELLS><<<gb, kStripeThreads, 0, s>>>(phi, rhs, ctl, a, R);
+}
+
+template <typename T, bool TRACK>
+int launch_stripes(T *phi, const T *rhs, Ctl *ctl, const SolveArgs &a, int R, int ns, dim3 gb, int cells,
+                   cudaStream_t s)
+{
+    if (cells <= 1) launch_stripes_c<T, TRACK, 1>(phi, rhs, ctl, a, R, ns, gb, s);
+    else if (cells <= 2) launch_stripes_c<T, TRACK, 2>(phi, rhs, ctl, a, R, ns, gb, s);
+    else if (cells <= 4) launch_stripes_c<T, TRACK, 4>(phi, rhs, ctl, a, R, ns, gb, s);
+    else launch_stripes_c<T, TRACK, kRowCellsMax>(phi, rhs, ctl, a, R, ns, gb, s);
+    return PCD_OK;
+}
+
 // Enqueues one chunk of `sweeps` sweeps (plus the checks that follow them) on s.
 template <bool MASKED>
 int enqueue_chunk(SolverWorkspace &ws, const double *b, double *phi, const SolveArgs &a, int precision,
-                  int sweeps, cudaStream_t s, int *nodes)
+                  int sweeps, cudaStream_t s, int *nodes, bool stripes)
 {
     const int half = (a.W + 1) >> 1;
     const int blocks = ceil_div((long)a.H * half, kThreads);
     const int rblocks = grid_blocks((long)a.W * a.H);
     const bool track = (a.stop == PCD_STOP_MAX_UPDATE);
     int n = 0;
+    if (!MASKED && stripes) {
+        const int R = stripe_rows(a.H, ws.stripe_resident);
+        const int ns = (a.H + R - 1) / R;
+        const dim3 gb(1, 2 * ns);  // one block per boundary row (relax_row strides over the row)
+        const int cells = ceil_div(half, kStripeThreads);
+        for (int k = 0; k < sweeps; k++) {
+            if (precision == PCD_PREC_MIXED) {
+                if (track) PCD_TRY((launch_stripes<float, true>(ws.e32, ws.r32, ws.ctl, a, R, ns, gb, cells, s)));
+                else PCD_TRY((launch_stripes<float, false>(ws.e32, ws.r32, ws.ctl, a, R, ns, gb, cells, s)));
+            } else {
+                if (track) PCD_TRY((launch_stripes<double, true>(phi, b, ws.ctl, a, R, ns, gb, cells, s)));
+                else PCD_TRY((launch_stripes<double, false>(phi, b, ws.ctl, a, R, ns, gb, cells, s)));
+            }
+            n += 2;
+        }
+        sweeps = 0;
+    }
     for (int k = 0; k < sweeps; k++) {
         for (int color = 0; color < 2; color++) {
             const int last = color == 1;
@@ -427,10 +595,10 @@ int enqueue_chunk(SolverWorkspace &ws, const double *b, double *phi, const Solve
 }
 
 int get_chunk_graph(SolverWorkspace &ws, const double *b, double *phi, const SolveArgs &a, int precision,
-                    int masked, int sweeps, cudaStream_t s, SolverWorkspace::GraphEntry **out)
+                    int masked, int sweeps, cudaStream_t s, SolverWorkspace::GraphEntry **out, bool stripes)
 {
     std::vector<long long> key = {(long long)(uintptr_t)b, (long long)(uintptr_t)phi, a.W, a.H, a.ld, a.stop,
-                                  a.max_iter, precision, masked, sweeps};
+                                  a.max_iter, precision, masked, sweeps, stripes ? 1 : 0};
     long long tb, ob;
     std::memcpy(&tb, &a.tol, 8);
     std::memcpy(&ob, &a.omega, 8);
@@ -444,8 +612,8 @@ int get_chunk_graph(SolverWorkspace &ws, const double *b, double *phi, const Sol
     cudaGraph_t g;
     int nodes = 0;
     PCD_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-    int st = masked ? enqueue_chunk<true>(ws, b, phi, a, precision, sweeps, s, &nodes)
-                    : enqueue_chunk<false>(ws, b, phi, a, precision, sweeps, s, &nodes);
+    int st = masked ? enqueue_chunk<true>(ws, b, phi, a, precision, sweeps, s, &nodes, false)
+                    : enqueue_chunk<false>(ws, b, phi, a, precision, sweeps, s, &nodes, stripes);
     cudaError_t ce = cudaStreamEndCapture(s, &g);
     if (st != PCD_OK) return st;
     if (ce != cudaSuccess) {
@@ -574,6 +742,7 @@ int solve_cluster(SolverWorkspace &ws, const double *b, double *phi, const Solve
     ca.tol = a.tol;
     ca.drop = 3e-2;
     for (int c = 0; c < 5; c++) ca.w32[c] = a.w32[c];
+    ca.one_minus_omega = (float)(1.0 - a.omega);
 
     PCD_CUDA(cudaEventRecord(ws.k0, s));
     long launched = 0;
@@ -675,7 +844,8 @@ int solve_device(SolverWorkspace &ws, const double *b, double *phi, int W, int H
         if (cluster_plan(ws.dev, W, H, &C, &smem, &khp) == PCD_OK)
             return solve_cluster(ws, b, phi, a, o, C, smem, khp, stats, s);
     }
-    if (!done_already && !masked && o.schedule != PCD_SCHED_LAUNCHES) {
+    if (!done_already && !masked &&
+        (o.schedule == PCD_SCHED_AUTO || o.schedule == PCD_SCHED_PERSISTENT || o.schedule == PCD_SCHED_CLUSTER)) {
         int G = 0;
         size_t smem = 0;
         if (persist_grid(ws.dev, W, H, precision == PCD_PREC_MIXED, &G, &smem) == PCD_OK)
@@ -696,17 +866,30 @@ int solve_device(SolverWorkspace &ws, const double *b, double *phi, int W, int H
         PCD_LAUNCHED(1);
     }
 
+    // fused stripe sweeps for grids with at least 3 rows and no NaN cells
+    const bool stripes = !masked && H >= 3 && W <= 2 * kRowCellsMax * kStripeThreads &&
+                         o.schedule != PCD_SCHED_LAUNCHES;
+    if (stripes && ws.stripe_resident == 0) {
+        int sms = 0, bps = 0;
+        PCD_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ws.dev));
+        PCD_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_stripe_a<double, false, 4>, kStripeThreads, 0));
+        ws.stripe_resident = std::max(1, bps) * sms;
+    }
     int chunk;
     if (a.stop == PCD_STOP_MAX_UPDATE)
         chunk = precision == PCD_PREC_MIXED ? (o.refine_every > 0 ? o.refine_every : 32) : 32;
     else if (precision == PCD_PREC_MIXED)
-        chunk = o.refine_every > 0 ? o.refine_every : (o.check_every > 0 ? o.check_every : 32);
+        // the FP64 refresh costs several FP32 sweeps; FP32 can carry ~2 digits
+        // of the correction, i.e. hundreds of sweeps on large grids
+        chunk = o.refine_every > 0 ? o.refine_every
+                                   : (o.check_every > 0 ? o.check_every
+                                                        : std::max(32, std::min(256, std::max(W, H) / 16)));
     else
         chunk = o.check_every > 0 ? o.check_every : 32;
     if (chunk > a.max_iter && a.max_iter > 0) chunk = a.max_iter;
 
     SolverWorkspace::GraphEntry *ge = nullptr;
-    if (!done_already) PCD_TRY(get_chunk_graph(ws, b, phi, a, precision, masked, chunk, s, &ge));
+    if (!done_already) PCD_TRY(get_chunk_graph(ws, b, phi, a, precision, masked, chunk, s, &ge, stripes));
 
     PCD_CUDA(cudaEventRecord(ws.k0, s));
     // Chunk loop: launch chunk i+1 before inspecting chunk i's control block.
@@ -756,7 +939,7 @@ int solve_device(SolverWorkspace &ws, const double *b, double *phi, int W, int H
         stats->device_ms = ms;
         cudaEventElapsedTime(&ms, ws.k0, ws.k1);
         stats->sweep_ms = ms;
-        stats->schedule_used = PCD_SCHED_LAUNCHES;
+        stats->schedule_used = stripes ? PCD_SCHED_STRIPES : PCD_SCHED_LAUNCHES;
     }
     return c.converged ? PCD_OK : PCD_NOT_CONVERGED;
 }

@@ -68,6 +68,7 @@ struct SolverWorkspace {
     size_t xbuf_elems = 0;
     unsigned *flags = nullptr;  // epoch flags + barrier counter
     int max_ctas = 0;
+    int stripe_resident = 0;    // resident stripe blocks (SMs x blocks per SM)
     double *part = nullptr;     // check partials
 
     struct GraphEntry {

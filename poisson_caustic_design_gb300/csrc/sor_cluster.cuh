@@ -19,6 +19,7 @@ struct ClusterArgs {
     double tol;          // relative stop tolerance
     double drop;         // end the cycle when the estimate fell by this factor
     float w32[5];        // omega / cnt
+    float one_minus_omega;
 };
 
 // Cluster size (16 or 8 CTAs) and dynamic shared memory for a W x H grid;

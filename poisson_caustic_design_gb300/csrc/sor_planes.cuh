@@ -1,0 +1,194 @@
+// sor_planes.cuh -- FP32 red-black SOR on colour planes split across the
+// CTAs of one thread-block cluster (internal; used by sor_cluster.cu and
+// sor_batch.cu).
+//
+// CTA g of a C-CTA cluster owns grid rows [r0, r0+n) (band_of).  Its state is
+// four FP32 planes with row stride KHp (even, >= ceil(W/2), multiple of 4):
+//   e0 / e1 : red / black cells of the correction e, rows 0..n+1 (0 and n+1
+//             are halo copies of the neighbouring CTAs' facing rows)
+//   r0 / r1 : red / black cells of the right-hand side r32, rows 0..n-1
+// Cell (x, y) of colour c = (x+y)&1 lives at e_c[(y - r0 + 1)*KHp + (x >> 1)].
+// In row y (p = y&1) the cell of colour c at slot k sits at x = 2k + (p^c); its
+// left / right neighbours (other colour) sit at slots k - q and k - q + 1 with
+// q = 1 - (p^c); its up / down neighbours at slot k of rows y-1, y+1.
+//
+// The planes live either in the CTA's shared memory (neighbours reached
+// through DSMEM) or in an L2-resident global scratch region laid out the same
+// way per CTA (neighbours read with ld.global.cg, ordered by the cluster
+// barrier's release/acquire).
+#pragma once
+
+#include <cooperative_groups.h>
+
+#include "common.cuh"
+
+namespace pcd {
+namespace planes {
+
+namespace cg = cooperative_groups;
+
+__device__ __forceinline__ void band_of(int g, int G, int H, int &r0, int &n)
+{
+    const int base = H / G, extra = H % G;
+    n = base + (g < extra ? 1 : 0);
+    r0 = g * base + (g < extra ? g : extra);
+}
+
+// Relaxation factors and grid size of one solve.
+struct Grid {
+    int W, H;
+    float w0, w1, w2, w3, w4;  // omega / cnt
+};
+
+struct Planes {
+    float *e0, *e1;  // red, black planes of e
+    float *r0, *r1;  // red, black planes of r32
+    int KHp;
+    int in_smem;     // 1: shared memory; 0: global scratch
+    long cta_stride; // global scratch: floats between consecutive CTAs' regions
+    __device__ __forceinline__ float *e(int c) const { return c ? e1 : e0; }
+    __device__ __forceinline__ float *r(int c) const { return c ? r1 : r0; }
+};
+
+__host__ __device__ inline int plane_stride(int W) { return ((W + 1) / 2 + 3) / 4 * 4; }
+
+// floats of one CTA's four planes for bands of at most nmax rows
+__host__ __device__ inline long planes_floats(int nmax, int KHp) { return (long)(2 * (nmax + 2) + 2 * nmax) * KHp; }
+
+__device__ __forceinline__ void carve(Planes &P, float *base, int nmax)
+{
+    const long plane = (long)(nmax + 2) * P.KHp, rplane = (long)nmax * P.KHp;
+    P.e0 = base;
+    P.e1 = base + plane;
+    P.r0 = base + 2 * plane;
+    P.r1 = base + 2 * plane + rplane;
+}
+
+// Copy the neighbours' facing rows of plane c into its halo rows.
+__device__ __forceinline__ void fetch_halo_plane(cg::cluster_group &cl, const Planes &P, int c, int g, int C, int n,
+                                                 int H)
+{
+    float *pl = P.e(c);
+    const int KHp = P.KHp, K4 = KHp >> 2;
+    if (g > 0) {
+        int pr0, pn;
+        band_of(g - 1, C, H, pr0, pn);
+        const float *nb = P.in_smem ? cl.map_shared_rank(pl, g - 1) : pl - P.cta_stride;
+        const float4 *src = reinterpret_cast<const float4 *>(nb + (size_t)pn * KHp);
+        float4 *dst = reinterpret_cast<float4 *>(pl);
+        if (P.in_smem)
+            for (int i = threadIdx.x; i < K4; i += blockDim.x) dst[i] = src[i];
+        else
+            for (int i = threadIdx.x; i < K4; i += blockDim.x) dst[i] = __ldcg(src + i);
+    }
+    if (g < C - 1) {
+        const float *nb = P.in_smem ? cl.map_shared_rank(pl, g + 1) : pl + P.cta_stride;
+        const float4 *src = reinterpret_cast<const float4 *>(nb + (size_t)KHp);
+        float4 *dst = reinterpret_cast<float4 *>(pl + (size_t)(n + 1) * KHp);
+        if (P.in_smem)
+            for (int i = threadIdx.x; i < K4; i += blockDim.x) dst[i] = src[i];
+        else
+            for (int i = threadIdx.x; i < K4; i += blockDim.x) dst[i] = __ldcg(src + i);
+    }
+}
+
+// One half sweep of colour c over the band: each thread owns slot pair
+// (k, k+1) of rows lr = 1 + rg, 1 + rg + RP, ...
+__device__ __forceinline__ void relax_pair(const Planes &P, int c, int n, int r0, const Grid &G, int k, int rg, int RP)
+{
+    const int W = G.W, H = G.H, KHp = P.KHp;
+    float *__restrict__ own = P.e(c);
+    const float *__restrict__ oth = P.e(c ^ 1);
+    const float *__restrict__ rhs = P.r(c);
+    const float w1 = G.w1, w2 = G.w2, w3 = G.w3, w4 = G.w4;
+#pragma unroll 2
+    for (int lr = 1 + rg; lr <= n; lr += RP) {
+        const int y = r0 + lr - 1;
+        const int s = (y & 1) ^ c;     // x = 2k + s
+        const int q = 1 - s;           // left neighbour slot = k - q
+        const size_t ro = (size_t)lr * KHp;
+        float2 v = *reinterpret_cast<float2 *>(own + ro + k);
+        const float2 rh = *reinterpret_cast<const float2 *>(rhs + ro - KHp + k);
+        const float2 up = *reinterpret_cast<const float2 *>(oth + ro - KHp + k);
+        const float2 dn = *reinterpret_cast<const float2 *>(oth + ro + KHp + k);
+        const float2 mid = *reinterpret_cast<const float2 *>(oth + ro + k);
+        const float extra = oth[ro + (q ? k - 1 : k + 2)];
+        const int x0 = 2 * k + s, x1 = x0 + 2;
+        if (y > 0 && y < H - 1 && x0 > 0 && x1 + 1 < W) {
+            // interior pair: four neighbours each; the reference's form
+            // v + w (sum - 4 v - r) forms the small correction first, which
+            // keeps FP32 rounding at the level of the change
+            float s0, s1;
+            if (q) { s0 = extra + mid.x; s1 = mid.x + mid.y; }
+            else { s0 = mid.x + mid.y; s1 = mid.y + extra; }
+            s0 += up.x + dn.x;
+            s1 += up.y + dn.y;
+            v.x = fmaf(w4, fmaf(-4.f, v.x, s0) - rh.x, v.x);
+            v.y = fmaf(w4, fmaf(-4.f, v.y, s1) - rh.y, v.y);
+        } else {
+            const float l0 = q ? extra : mid.x, r0v = q ? mid.x : mid.y;
+            const float l1 = q ? mid.x : mid.y, r1v = q ? mid.y : extra;
+            const bool hu = y > 0, hd = y < H - 1;
+            const float vert0 = (hu ? up.x : 0.f) + (hd ? dn.x : 0.f);
+            const float vert1 = (hu ? up.y : 0.f) + (hd ? dn.y : 0.f);
+            const int cv = (int)hu + (int)hd;
+            if (x0 < W) {
+                const bool hl = x0 > 0, hr = x0 + 1 < W;
+                const float sum = vert0 + (hl ? l0 : 0.f) + (hr ? r0v : 0.f);
+                const int cnt = cv + (int)hl + (int)hr;
+                const float w = cnt == 4 ? w4 : cnt == 3 ? w3 : cnt == 2 ? w2 : cnt == 1 ? w1 : G.w0;
+                v.x = v.x + w * (sum - (float)cnt * v.x - rh.x);
+            }
+            if (x1 < W) {
+                const bool hr = x1 + 1 < W;  // x1 >= 2 always has a left neighbour
+                const float sum = vert1 + l1 + (hr ? r1v : 0.f);
+                const int cnt = cv + 1 + (int)hr;
+                const float w = cnt == 4 ? w4 : cnt == 3 ? w3 : cnt == 2 ? w2 : w1;
+                v.y = v.y + w * (sum - (float)cnt * v.y - rh.y);
+            }
+        }
+        *reinterpret_cast<float2 *>(own + ro + k) = v;
+    }
+}
+
+// Sum over own cells of (r32 - L e)^2, both colours; FP32 per thread (a few
+// dozen cells), FP64 across threads -- the FP64 pipe of this part is 1/56 of
+// the FP32 one, so per-cell FP64 arithmetic would dominate the check.
+__device__ __forceinline__ double residual_sq(const Planes &P, int n, int r0, const Grid &G)
+{
+    const int W = G.W, H = G.H, KHp = P.KHp;
+    float acc = 0.f;
+    for (int t = threadIdx.x; t < n * W; t += blockDim.x) {
+        const int row = t / W, x = t - row * W, y = r0 + row;
+        const int c = (x + y) & 1, kk = x >> 1;
+        const size_t ro = (size_t)(row + 1) * KHp;
+        const float *oth = P.e(c ^ 1);
+        const int s = (y & 1) ^ c, q = 1 - s;
+        float sum = 0.f;
+        int cnt = 0;
+        if (x > 0) { sum += oth[ro + kk - q]; cnt++; }
+        if (x < W - 1) { sum += oth[ro + kk - q + 1]; cnt++; }
+        if (y > 0) { sum += oth[ro - KHp + kk]; cnt++; }
+        if (y < H - 1) { sum += oth[ro + KHp + kk]; cnt++; }
+        const float e = P.e(c)[ro + kk];
+        const float r = P.r(c)[ro - KHp + kk] - (sum - (float)cnt * e);
+        acc = fmaf(r, r, acc);
+    }
+    return (double)acc;
+}
+
+// Block-wide sum into thread 0 (blockDim a multiple of 32).
+__device__ __forceinline__ double block_sum(double v, double *s_red)
+{
+    v = warp_sum(v);
+    if ((threadIdx.x & 31) == 0) s_red[threadIdx.x >> 5] = v;
+    __syncthreads();
+    double t = 0.0;
+    if (threadIdx.x == 0)
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += s_red[w];
+    __syncthreads();
+    return t;
+}
+
+}  // namespace planes
+}  // namespace pcd

@@ -19,13 +19,13 @@ from dataclasses import dataclass
 import numpy as np
 
 from . import _lib
-from ._lib import (PREC_FP64, PREC_MIXED, SCHED_AUTO, SCHED_CLUSTER, SCHED_LAUNCHES, SCHED_PERSISTENT,
+from ._lib import (PREC_FP64, PREC_MIXED, SCHED_AUTO, SCHED_CLUSTER, SCHED_LAUNCHES, SCHED_PERSISTENT, SCHED_STRIPES,
                    STOP_MAX_UPDATE,
                    STOP_REL_RESIDUAL, check)
 
-__all__ = ["poisson_solver", "solver_progress", "Context", "SolveOptions", "PREC_FP64", "PREC_MIXED",
+__all__ = ["poisson_solver", "batch_solve", "solver_progress", "Context", "SolveOptions", "PREC_FP64", "PREC_MIXED",
            "STOP_MAX_UPDATE", "STOP_REL_RESIDUAL", "SCHED_AUTO", "SCHED_LAUNCHES", "SCHED_PERSISTENT",
-           "SCHED_CLUSTER"]
+           "SCHED_CLUSTER", "SCHED_STRIPES"]
 
 # solver.h:10 declares `extern double solver_progress`; the reference never
 # updates it (solver.cpp:9,63-68), so neither does this mirror.
@@ -131,6 +131,34 @@ class Context:
         d = st.as_dict()
         d["status"] = s
         return d
+
+
+def batch_solve(ctx: Context, bs, phis, opts: SolveOptions | None = None, stream=None):
+    """Solve many independent grids (CUDA float64 tensors, 2-D, unit column
+    stride, of any sizes) in one persistent launch.  Returns (per-instance
+    stats, batch stats)."""
+    import torch
+
+    if len(bs) != len(phis) or not bs:
+        raise ValueError("need equally many right-hand sides and solutions")
+    arr = (_lib.Instance * len(bs))()
+    for i, (b, p) in enumerate(zip(bs, phis)):
+        if not (isinstance(b, torch.Tensor) and b.is_cuda and b.dtype == torch.float64 and b.dim() == 2
+                and b.stride(1) == 1 and p.shape == b.shape and p.stride() == b.stride()):
+            raise TypeError("instances must be 2-D float64 CUDA tensors with unit column stride, b and phi alike")
+        arr[i].width, arr[i].height, arr[i].ld = b.shape[1], b.shape[0], b.stride(0)
+        arr[i].b, arr[i].phi = b.data_ptr(), p.data_ptr()
+    o = (opts or SolveOptions(stop=STOP_REL_RESIDUAL, tol=1e-6, omega=-1.0)).to_c()
+    st = (_lib.InstanceStats * len(bs))()
+    bst = _lib.BatchStats()
+    if stream is None:
+        stream = torch.cuda.current_stream(bs[0].device).cuda_stream
+    L = _lib.load()
+    s = check(L.pcd_batch_solve_device(ctx.handle, arr, len(bs), C.byref(o), st, C.byref(bst),
+                                       C.c_void_p(int(stream))), "pcd_batch_solve_device",
+              (_lib.PCD_OK, _lib.PCD_NOT_CONVERGED))
+    per = [{k: getattr(x, k) for k, _ in x._fields_} for x in st]
+    return per, {**{k: getattr(bst, k) for k, _ in bst._fields_}, "status": s}
 
 
 def poisson_solver(D, phi, width: int, height: int, max_iterations: int, convergence_threshold: float,

@@ -1,0 +1,65 @@
+"""The batched solve (many grids of uneven sizes in one persistent cluster
+launch) against the exact DCT solve and against the single-grid solver."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+SIZES = [(64, 64), (96, 96), (128, 128), (256, 256), (512, 512), (1024, 1024), (300, 200), (97, 33), (640, 480),
+         (64, 700)]
+
+
+def test_batch_matches_exact_and_single_solves(ctx):
+    import torch
+
+    import oracle
+    import poisson_caustic_design_gb300 as pcd
+
+    rhs = [pcd.inputs.poisson_rhs(w, 40 + i, "gaussian" if i % 2 else "binary", m=h) for i, (w, h) in enumerate(SIZES)]
+    bs = [torch.from_numpy(b).cuda() for b in rhs]
+    phis = [torch.full_like(b, 7.0) for b in bs]           # garbage: warm_start=False must ignore it
+    opts = pcd.SolveOptions(stop=pcd.STOP_REL_RESIDUAL, tol=1e-8, max_iterations=200000, omega=-1.0,
+                            warm_start=False)
+    per, bst = pcd.batch_solve(ctx, bs, phis, opts)
+    torch.cuda.synchronize()
+    assert bst["status"] == 0 and bst["clusters"] >= 1
+    port = oracle.Port()
+    for i, (b, p) in enumerate(zip(rhs, phis)):
+        assert per[i]["converged"] == 1, (SIZES[i], per[i])
+        phi = p.cpu().numpy()
+        _, rn, bn, _ = port.residual(b, phi)
+        assert rn / bn <= 1.05e-8, (SIZES[i], rn / bn, per[i])
+        assert abs(rn / bn - per[i]["rel_residual"]) <= 1e-3 * per[i]["rel_residual"] + 1e-15
+        e2, _ = oracle.rel_err_mod_const(phi, oracle.dct_solve(b))
+        assert e2 < 1e-6, (SIZES[i], e2)
+    # the same grid through the single-grid solver agrees to the tolerance
+    single = np.zeros_like(rhs[4])
+    ctx.solve(rhs[4], single, pcd.SolveOptions(stop=pcd.STOP_REL_RESIDUAL, tol=1e-8, omega=-1.0,
+                                               precision=pcd.PREC_MIXED))
+    assert oracle.rel_err_mod_const(phis[4].cpu().numpy(), single)[0] < 1e-6
+
+
+def test_batch_graph_replay_is_repeatable(ctx):
+    import torch
+
+    import poisson_caustic_design_gb300 as pcd
+
+    bs = [torch.from_numpy(pcd.inputs.poisson_rhs(n, n, "gaussian")).cuda() for n in (64, 128, 256)]
+    phis = [torch.zeros_like(b) for b in bs]
+    opts = pcd.SolveOptions(stop=pcd.STOP_REL_RESIDUAL, tol=1e-6, omega=-1.0, warm_start=False)
+    per1, _ = pcd.batch_solve(ctx, bs, phis, opts)
+    first = [p.clone() for p in phis]
+    per2, _ = pcd.batch_solve(ctx, bs, phis, opts)
+    for a, b in zip(first, phis):
+        assert torch.equal(a, b)       # same schedule per cluster: deterministic per instance
+    assert [x["sweeps"] for x in per1] == [x["sweeps"] for x in per2]
+
+
+def test_batch_rejects_bad_instances(ctx):
+    import torch
+
+    import poisson_caustic_design_gb300 as pcd
+
+    b = torch.zeros((16, 16), dtype=torch.float64, device="cuda")
+    with pytest.raises(pcd.PCDError):
+        pcd.batch_solve(ctx, [b], [torch.zeros_like(b)])      # height < 32

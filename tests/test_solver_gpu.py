@@ -16,7 +16,7 @@ from conftest import load_golden, solver_case_names
 pytestmark = pytest.mark.gpu
 
 RTOL_PLAIN = 1e-5
-SCHEDS = [1, 2]  # launch-per-half-sweep, persistent
+SCHEDS = [1, 2]  # launch-per-half-sweep, persistent (4 = fused stripes, 3 = cluster)
 
 
 def _rel_mod_const(x, ref):
@@ -64,20 +64,36 @@ def test_stats_and_reference_stop_semantics(ctx, sched, prec):
     assert st["sweeps"] == 37 and st["converged"] == 0 and st["status"] == 1
 
 
-@pytest.mark.parametrize("n,m", [(512, 512), (300, 200), (1024, 1024)])
+@pytest.mark.parametrize("n,m", [(512, 512), (300, 200), (1024, 1024), (257, 3), (33, 700)])
 def test_persistent_and_launch_schedules_agree(ctx, n, m):
-    """Both schedules run the same red-black iteration: after the same fixed
-    number of FP64 sweeps the iterates agree to rounding."""
+    """All FP64 schedules run the same red-black iteration: after the same
+    fixed number of sweeps the iterates agree to rounding."""
     import poisson_caustic_design_gb300 as pcd
 
     b = pcd.inputs.poisson_rhs(n, 5, "binary", m=m)
     out = []
-    for sched in SCHEDS:
+    for sched in SCHEDS + [4]:
         phi = np.zeros_like(b)
         st = ctx.solve(b, phi, pcd.SolveOptions(tol=0.0, max_iterations=200, schedule=sched, omega=-1.0))
         assert st["sweeps"] == 200
         out.append(phi)
-    assert np.abs(out[0] - out[1]).max() <= 1e-9 * np.abs(out[0]).max()
+    for o in out[1:]:
+        assert np.abs(out[0] - o).max() <= 1e-9 * np.abs(out[0]).max()
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+def test_stripes_on_grid_beyond_chip(ctx, prec):
+    """A grid too large for the on-chip schedules runs the fused stripe
+    sweeps and reaches the exact solve."""
+    import oracle
+    import poisson_caustic_design_gb300 as pcd
+
+    b = pcd.inputs.poisson_rhs(2048, 6, "gaussian", m=1800)
+    phi = np.zeros_like(b)
+    st = ctx.solve(b, phi, pcd.SolveOptions(stop=pcd.STOP_REL_RESIDUAL, tol=1e-8, max_iterations=100000,
+                                            omega=-1.0, precision=prec))
+    assert st["converged"] and st["schedule_used"] == 4   # 1800/148 rows x 2048 x 16 B exceed shared memory
+    assert _rel_mod_const(phi, oracle.dct_solve(b))[0] < 1e-6
 
 
 @pytest.mark.parametrize("sched", SCHEDS)
