@@ -48,6 +48,7 @@ def parse():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--cpu-budget-s", type=float, default=20.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-batch", action="store_true")
     return ap.parse_args()
 
 
@@ -225,10 +226,21 @@ def run_ours(args, rank, world, local, pg):
 
     forms = {
         "mixed": pcd.SolveOptions(stop=pcd.STOP_REL_RESIDUAL, tol=TOL, max_iterations=200000,
-                                  precision=pcd.PREC_MIXED, omega=-1.0, warm_start=False),
+                                  precision=pcd.PREC_MIXED, omega=-1.0, warm_start=0),
         "plain_fp64": pcd.SolveOptions(stop=pcd.STOP_REL_RESIDUAL, tol=TOL, max_iterations=200000,
-                                       precision=pcd.PREC_FP64, omega=-1.0, warm_start=False),
+                                       precision=pcd.PREC_FP64, omega=-1.0, warm_start=0),
     }
+    from poisson_caustic_design_gb300 import learned as _learned
+
+    wpath = _learned.default_weights_path(256)
+    net = None
+    if os.path.exists(wpath):
+        net = _learned.UNet(ctx, resolution=256, max_batch=1)
+        net.load(wpath)
+        net.attach(ctx)
+        forms = {"learned_mixed": pcd.SolveOptions(stop=pcd.STOP_REL_RESIDUAL, tol=TOL, max_iterations=200000,
+                                                   precision=pcd.PREC_MIXED, omega=-1.0, warm_start=2), **forms}
+    headline = "learned_mixed" if net is not None else "mixed"
 
     def timed(opts, k):
         b = bs[k % len(bs)]
@@ -248,24 +260,27 @@ def run_ours(args, rank, world, local, pg):
             timed(opts, w)
         torch.cuda.synchronize()
         barrier(pg)
-        if name == "mixed":
+        if name == headline:
             sampler.start()
             launches_before = L.pcd_kernel_launches()
-        ms, sweeps, sweep_ms, rels = [], [], [], []
+        ms, sweeps, sweep_ms, rels, warm = [], [], [], [], []
         for k in range(args.steps):
             t, st = timed(opts, k)
             ms.append(t)
             sweeps.append(st["sweeps"])
             sweep_ms.append(st["sweep_ms"])
             rels.append(st["rel_residual"])
+            warm.append(st["warm_used"])
         torch.cuda.synchronize()
         barrier(pg)
-        if name == "mixed":
+        if name == headline:
             launches = L.pcd_kernel_launches() - launches_before
             clocks = sampler.stop()
         results[name] = {"ms": max_over_ranks(pg, float(np.sum(ms))) / args.steps, "sweeps": float(np.mean(sweeps)),
                          "sweep_ms": float(np.mean(sweep_ms)), "max_rel_residual": float(np.max(rels)),
                          "schedule": int(st["schedule_used"])}
+        if name == "learned_mixed":
+            results[name]["warm_accepted"] = int(sum(w == 2 for w in warm))
 
     # accuracy against an FP64 solve to 1e-12 (the plain FP64 solver, itself
     # checked against the exact DCT solve in the tests) -- outside timing
@@ -283,7 +298,7 @@ def run_ours(args, rank, world, local, pg):
         acc[name] = {"l2": float(d.norm() / r.norm()), "max": float(d.abs().max() / r.abs().max())}
 
     # end to end through the host-array C ABI: pinned b in, phi out
-    mixed = forms["mixed"]
+    mixed = forms[headline]
     hb = [torch.from_numpy(b).pin_memory() for b in bs_host]
     hphi = torch.zeros((N_GRID, N_GRID), dtype=torch.float64).pin_memory()
     for w in range(args.warmup):
@@ -302,6 +317,7 @@ def run_ours(args, rank, world, local, pg):
     # roofline of the dominant kernel: the persistent FP32 sweep kernel.
     # Algorithmic bytes per cell-sweep: 12 (read e, read r32, write e in FP32).
     m = results["mixed"]
+    hm = results[headline]
     cells = N_GRID * N_GRID
     alg_bytes = 12.0 * cells * m["sweeps"]
     achieved = alg_bytes / (m["sweep_ms"] * 1e-3) / 1e9
@@ -316,6 +332,53 @@ def run_ours(args, rank, world, local, pg):
             "traffic": None, "peak_source": "measured" if "hbm_gbs" in peaks else "fallback",
             "kernel": "k_sor_cluster (FP32 sweeps)", "alg_bytes_per_solve": alg_bytes,
             "note": "512^2 working set is shared-memory resident; DRAM traffic per launch is the band load/store"}
+
+    # batched configuration: 64 instances, sizes uniform in {64..1024}^2, one
+    # persistent cluster launch (CUDA graph); FP32 sweeps, FP64 residuals
+    batched = None
+    if not args.no_batch:
+        rs = np.random.default_rng(2024)
+        sizes = [int(rs.choice([64, 96, 128, 256, 512, 1024])) for _ in range(64)]
+        bb = [pcd.inputs.poisson_rhs_torch(n_, [5000 + i])[0].contiguous() for i, n_ in enumerate(sizes)]
+        pp = [torch.zeros_like(x) for x in bb]
+        bopts = pcd.SolveOptions(stop=pcd.STOP_REL_RESIDUAL, tol=TOL, max_iterations=200000, omega=-1.0, warm_start=0)
+        for w in range(max(1, args.warmup // 2)):
+            pcd.batch_solve(ctx, bb, pp, bopts)
+        bt = []
+        for k in range(max(2, args.steps // 2)):
+            flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            per, bst = pcd.batch_solve(ctx, bb, pp, bopts, stream=stream.cuda_stream)
+            e1.record(stream)
+            e1.synchronize()
+            bt.append(e0.elapsed_time(e1))
+        bms = float(np.mean(bt))
+        batched = {"instances": 64, "sizes": {str(n_): sizes.count(n_) for n_ in sorted(set(sizes))},
+                   "ms_per_batch": bms, "solves_per_s": 64 / (bms * 1e-3),
+                   "alg_gbs": 12.0 * bst["cell_sweeps"] / (bms * 1e-3) / 1e9,
+                   "all_converged": bool(all(x["converged"] for x in per)),
+                   "max_rel_residual": float(max(x["rel_residual"] for x in per)),
+                   "clusters": bst["clusters"], "cluster_size": bst["cluster_size"]}
+        del bb, pp
+
+    # HBM-bound sweep roofline: fused red+black stripe sweeps on 4096^2 (FP32
+    # 12 B and FP64 24 B algorithmic per cell-sweep), 256 sweeps per solve
+    stream_roof = None
+    if not args.no_batch:
+        n4 = 4096
+        b4 = pcd.inputs.poisson_rhs_torch(n4, [77])[0].contiguous()
+        p4 = torch.zeros_like(b4)
+        stream_roof = {}
+        for prec, bpc, nm in ((pcd.PREC_MIXED, 12, "fp32_sweeps"), (pcd.PREC_FP64, 24, "fp64_sweeps")):
+            o4 = pcd.SolveOptions(stop=pcd.STOP_REL_RESIDUAL, tol=0.0, max_iterations=256, omega=-1.0, precision=prec,
+                                  warm_start=0, schedule=pcd.SCHED_STRIPES, refine_every=256)
+            ctx.solve_device(b4, p4, o4, stream=stream.cuda_stream)
+            st4 = ctx.solve_device(b4, p4, o4, stream=stream.cuda_stream)
+            per_sweep = st4["sweep_ms"] * 1e-3 / st4["sweeps"]
+            ach = bpc * n4 * n4 / per_sweep / 1e9
+            stream_roof[nm] = {"us_per_sweep": per_sweep * 1e6, "achieved_gbs": ach, "frac_hbm": ach / peak}
+        del b4, p4
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -333,16 +396,21 @@ def run_ours(args, rank, world, local, pg):
                           f"tile-threaded SOR schedule on {seg * seg} threads")}
 
     line = {
-        "metric": METRIC, "value": m["ms"], "unit": UNIT, "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": m["ms"], "higher_is_better": False, "scaling": "weak",
+        "metric": METRIC, "value": hm["ms"], "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": hm["ms"], "higher_is_better": False, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32 sweeps + f64 residual/update", "data": "synthetic (seeded densities)",
-        "config": {"workload": "single 512x512 Neumann Poisson solve to rel residual 1e-6 (FP32 sweeps + FP64 "
-                               "defect correction)", "grid": N_GRID, "tol": TOL, "omega": "neumann-optimal",
+        "config": {"workload": "single 512x512 Neumann Poisson solve to rel residual 1e-6 (" +
+                               ("learned U-Net warm start + " if headline == "learned_mixed" else "") +
+                               "FP32 sweeps + FP64 defect correction)", "grid": N_GRID, "tol": TOL,
+                   "omega": "neumann-optimal",
                    "l2": "flushed before every solve (512 MiB write)", "instances": len(SEEDS),
                    "schedule": {1: "launches", 2: "persistent", 3: "cluster"}.get(m["schedule"], "?")},
         "forms": {k: {**v, "err_vs_fp64_1e-12": acc[k]} for k, v in results.items()},
         "speedup_plain_over_mixed": results["plain_fp64"]["ms"] / m["ms"],
-        "learned": None,
+        "speedup_plain_over_headline": results["plain_fp64"]["ms"] / hm["ms"],
+        "headline_form": headline,
+        "batched": batched,
+        "roofline_stream_4096": stream_roof,
         "roofline": roof,
         "cpu_baseline": cpu,
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": cells * 8, "d2h_bytes_per_step": cells * 8},

@@ -71,9 +71,19 @@ typedef struct {
                                 check_every sweeps (default 8 FP64 / 16 mixed), so it may run
                                 up to check_every-1 sweeps past the first passing sweep */
     int refine_every;        /* FP32 sweeps between FP64 residual replacements (mixed); 0 = auto */
-    int warm_start;          /* 1: phi holds the initial guess (reference behaviour); 0: start at 0 */
+    int warm_start;          /* pcd_warm_start: 1 phi holds the initial guess (reference
+                                behaviour); 0 start at 0; 2 the learned prediction */
     int schedule;            /* pcd_schedule */
 } pcd_solve_opts;
+
+typedef enum {
+    PCD_WARM_ZERO = 0,
+    PCD_WARM_GIVEN = 1,
+    /* the context's network (pcd_ctx_set_warm_start_net) predicts phi from b;
+     * the prediction is kept only if its residual is below ||b|| (a zero
+     * guess), otherwise the solve starts from zero (stats->warm_used = 3) */
+    PCD_WARM_LEARNED = 2
+} pcd_warm_start;
 
 typedef enum {
     PCD_SCHED_AUTO = 0,        /* cluster, else persistent, else launches, as the grid allows */
@@ -97,7 +107,9 @@ typedef struct {
     double device_ms;        /* device time of the solve (CUDA events) */
     int residual_checks;     /* FP64 residual evaluations */
     double sweep_ms;         /* device time of the sweep kernel(s) alone (CUDA events) */
-    int schedule_used;       /* pcd_schedule that ran (1 launches, 2 persistent) */
+    int schedule_used;       /* pcd_schedule that ran */
+    int warm_used;           /* 0 zero, 1 given, 2 learned, 3 learned prediction rejected (zero) */
+    double warm_rel_residual;/* ||b - L phi0|| / ||b|| of the learned prediction (warm_start 2) */
 } pcd_solve_stats;
 
 typedef struct pcd_ctx pcd_ctx;
@@ -129,8 +141,12 @@ int pcd_poisson_solver(const double *D, double *phi, int width, int height, int 
 int pcd_poisson_solve(pcd_ctx *ctx, const double *b, double *phi, int width, int height,
                       const pcd_solve_opts *opts, pcd_solve_stats *stats);
 
-/* Device arrays with leading dimension ld (elements, >= width) on `stream`
- * (NULL = the context's stream).  b is read, phi updated in place. */
+/* Device arrays with leading dimension ld (elements, >= width).  `stream` is
+ * the caller's stream (NULL = the CUDA default stream): the library works on
+ * the context's own stream, ordered after everything already enqueued on
+ * `stream` and before anything enqueued on it after the call.  The same
+ * holds for every entry point below that takes a stream.  b is read, phi
+ * updated in place. */
 int pcd_poisson_solve_device(pcd_ctx *ctx, const double *b, double *phi, int width, int height,
                              int ld, const pcd_solve_opts *opts, pcd_solve_stats *stats,
                              void *stream);
@@ -165,6 +181,34 @@ typedef struct {
  * whole.  stats has `count` entries in the caller's order. */
 int pcd_batch_solve_device(pcd_ctx *ctx, const pcd_instance *inst, int count, const pcd_solve_opts *opts,
                            pcd_instance_stats *stats, pcd_batch_stats *batch_stats, void *stream);
+
+/* ---- learned warm start (no counterpart in the reference) ------------------
+ * A 4-level BF16 U-Net (1->32->64->128->256 channels, 3x3 convolutions, FP32
+ * accumulation on the tensor cores) that maps a normalised right-hand side
+ * x = (b - mean b) / std(b) on a resolution x resolution grid to
+ * phi_hat = phi / (std(b) * resolution^2) with the mean removed.  Training and
+ * inference run the library's own kernels.  x, target, out: device FP32,
+ * batch x resolution x resolution. */
+typedef struct pcd_unet pcd_unet;
+int pcd_unet_create(pcd_ctx *ctx, int resolution, int max_batch, unsigned long long seed, pcd_unet **out);
+int pcd_unet_destroy(pcd_unet *net);
+long long pcd_unet_num_params(pcd_unet *net);
+int pcd_unet_resolution(pcd_unet *net);
+int pcd_unet_get_params(pcd_unet *net, float *host);
+int pcd_unet_set_params(pcd_unet *net, const float *host);
+/* one AdamW step on the mean squared error of the mean-removed prediction */
+int pcd_unet_train_step(pcd_unet *net, const float *x, const float *target, int batch, float lr,
+                        float weight_decay, float *loss, void *stream);
+int pcd_unet_predict(pcd_unet *net, const float *x, int batch, float *out, void *stream);
+/* gradients of the last training step (FP32, pcd_unet_num_params values) */
+int pcd_unet_get_grads(pcd_unet *net, float *host);
+/* The tensor-core GEMM the network is built on: C[M x N] (FP32, row stride
+ * ldc) = A[M x K] * B[N x K]^T with A, B BF16 row-major, K a multiple of 32,
+ * lda/ldb multiples of 8; ksplit > 1 needs ksplit*M*N floats of partials. */
+int pcd_gemm_bf16(const void *A, int lda, const void *B, int ldb, float *C, int ldc, int M, int N, int K,
+                  int ksplit, float *partials, void *stream);
+/* network used by warm_start = PCD_WARM_LEARNED (not owned; NULL clears) */
+int pcd_ctx_set_warm_start_net(pcd_ctx *ctx, pcd_unet *net);
 
 /* ---- grid utilities on device arrays (dense, ld == width) -------------- */
 int pcd_subtract_average_device(pcd_ctx *ctx, double *g, int width, int height, void *stream);

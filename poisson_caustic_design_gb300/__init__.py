@@ -14,8 +14,4 @@ from .solver import (PREC_FP64, PREC_MIXED, SCHED_AUTO, SCHED_CLUSTER, SCHED_LAU
                      SCHED_PERSISTENT, SCHED_STRIPES,
                      STOP_MAX_UPDATE, STOP_REL_RESIDUAL, Context, SolveOptions, batch_solve, poisson_solver,
                      solver_progress)
-
-try:  # the design mirror is optional until its library part is present
-    from .caustic_design import CausticDesign  # noqa: F401
-except ImportError:  # pragma: no cover
-    pass
+from .caustic_design import CausticDesign  # noqa: F401

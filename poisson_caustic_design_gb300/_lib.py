@@ -33,6 +33,9 @@ SCHED_LAUNCHES = 1
 SCHED_PERSISTENT = 2
 SCHED_CLUSTER = 3
 SCHED_STRIPES = 4
+WARM_ZERO = 0
+WARM_GIVEN = 1
+WARM_LEARNED = 2
 
 
 class PCDError(RuntimeError):
@@ -66,6 +69,8 @@ class SolveStats(C.Structure):
         ("residual_checks", C.c_int),
         ("sweep_ms", C.c_double),
         ("schedule_used", C.c_int),
+        ("warm_used", C.c_int),
+        ("warm_rel_residual", C.c_double),
     ]
 
     def as_dict(self):
@@ -122,6 +127,18 @@ SIGNATURES = {
     "pcd_gradient_device": (C.c_int, [_vp, _vp, _vp, _vp, C.c_int, C.c_int, _vp]),
     "pcd_divergence_device": (C.c_int, [_vp, _vp, _vp, _vp, C.c_int, C.c_int, _vp]),
     "pcd_subtract_average_noalloc": (C.c_int, [_vp, C.c_int, C.c_int, _vp]),
+    "pcd_unet_create": (C.c_int, [_vp, C.c_int, C.c_int, C.c_ulonglong, C.POINTER(_vp)]),
+    "pcd_unet_destroy": (C.c_int, [_vp]),
+    "pcd_unet_num_params": (C.c_longlong, [_vp]),
+    "pcd_unet_resolution": (C.c_int, [_vp]),
+    "pcd_unet_get_params": (C.c_int, [_vp, _vp]),
+    "pcd_unet_set_params": (C.c_int, [_vp, _vp]),
+    "pcd_unet_get_grads": (C.c_int, [_vp, _vp]),
+    "pcd_unet_train_step": (C.c_int, [_vp, _vp, _vp, C.c_int, C.c_float, C.c_float, C.POINTER(C.c_float), _vp]),
+    "pcd_unet_predict": (C.c_int, [_vp, _vp, C.c_int, _vp, _vp]),
+    "pcd_ctx_set_warm_start_net": (C.c_int, [_vp, _vp]),
+    "pcd_gemm_bf16": (C.c_int, [_vp, C.c_int, _vp, C.c_int, _vp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _vp,
+                                _vp]),
     "pcd_design_params_default": (C.c_int, [C.POINTER(DesignParams)]),
     "pcd_design_create": (C.c_int, [_vp, C.POINTER(DesignParams), C.POINTER(_vp)]),
     "pcd_design_destroy": (C.c_int, [_vp]),

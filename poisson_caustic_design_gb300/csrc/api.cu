@@ -11,6 +11,7 @@
 
 #include "api_internal.cuh"
 #include "design.cuh"
+#include "unet.cuh"
 
 namespace pcd {
 
@@ -37,10 +38,59 @@ int ctx_stage(pcd_ctx *ctx, size_t cells)
     return PCD_OK;
 }
 
+int StreamJoin::begin()
+{
+    if (user == work) return PCD_OK;
+    PCD_CUDA(cudaEventRecord(ctx->join_in, user));
+    PCD_CUDA(cudaStreamWaitEvent(work, ctx->join_in, 0));
+    return PCD_OK;
+}
+
+int StreamJoin::end()
+{
+    if (user == work) return PCD_OK;
+    PCD_CUDA(cudaEventRecord(ctx->join_out, work));
+    PCD_CUDA(cudaStreamWaitEvent(user, ctx->join_out, 0));
+    return PCD_OK;
+}
+
 int ctx_activate(pcd_ctx *ctx)
 {
     PCD_CUDA(cudaSetDevice(ctx->device));
     return PCD_OK;
+}
+
+// Solve with the warm-start policy of o: the learned prediction is kept only
+// when its FP64 residual is below that of a zero guess (||b||).
+int solve_with_warm_start(pcd_ctx *ctx, const double *b, double *phi, int W, int H, int ld, pcd_solve_opts o,
+                          pcd_solve_stats *stats, cudaStream_t s)
+{
+    int used = o.warm_start == PCD_WARM_GIVEN ? 1 : 0;
+    double rel0 = -1.0;
+    if (o.warm_start == PCD_WARM_LEARNED) {
+        if (!ctx->net) {
+            set_error("warm_start = PCD_WARM_LEARNED needs a network (pcd_ctx_set_warm_start_net)");
+            return PCD_BAD_ARG;
+        }
+        PCD_TRY(ctx->net->net.warm_start(b, W, H, ld, phi, s));
+        PCD_TRY(residual_rel(ctx->solver, b, phi, W, H, ld, s, &rel0));
+        if (rel0 < 1.0) {
+            used = 2;
+        } else {  // not better than a zero guess (or not finite): start from zero
+            PCD_TRY(zero_grid(phi, W, H, ld, s));
+            used = 3;
+        }
+        o.warm_start = PCD_WARM_GIVEN;
+    } else if (o.warm_start != PCD_WARM_ZERO && o.warm_start != PCD_WARM_GIVEN) {
+        set_error("pcd solve: unknown warm_start");
+        return PCD_BAD_ARG;
+    }
+    int st = solve_device(ctx->solver, b, phi, W, H, ld, o, stats, s);
+    if (stats) {
+        stats->warm_used = used;
+        stats->warm_rel_residual = rel0;
+    }
+    return st;
 }
 
 }  // namespace pcd
@@ -104,6 +154,8 @@ int pcd_ctx_create(int device, pcd_ctx **out)
     c->device = device;
     c->solver.dev = device;
     cudaError_t ce = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    if (ce == cudaSuccess) ce = cudaEventCreateWithFlags(&c->join_in, cudaEventDisableTiming);
+    if (ce == cudaSuccess) ce = cudaEventCreateWithFlags(&c->join_out, cudaEventDisableTiming);
     if (ce != cudaSuccess) {
         delete c;
         set_error(std::string("cudaStreamCreate: ") + cudaGetErrorString(ce));
@@ -119,11 +171,14 @@ int pcd_ctx_destroy(pcd_ctx *ctx)
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
     design_detach_all(ctx);
+    unet_detach_all(ctx);
     ctx->solver.release();
     ctx->grid.release();
     ctx->batch.release();
     if (ctx->d_b) cudaFree(ctx->d_b);
     if (ctx->d_phi) cudaFree(ctx->d_phi);
+    if (ctx->join_in) cudaEventDestroy(ctx->join_in);
+    if (ctx->join_out) cudaEventDestroy(ctx->join_out);
     cudaStreamDestroy(ctx->stream);
     delete ctx;
     return PCD_OK;
@@ -139,8 +194,11 @@ int pcd_poisson_solve_device(pcd_ctx *ctx, const double *b, double *phi, int wid
     PCD_TRY(ctx_activate(ctx));
     pcd_solve_opts o;
     if (opts) o = *opts; else pcd_solve_opts_default(&o);
-    cudaStream_t s = stream ? (cudaStream_t)stream : ctx->stream;
-    return solve_device(ctx->solver, b, phi, width, height, ld, o, stats, s);
+    StreamJoin j(ctx, stream);
+    PCD_TRY(j.begin());
+    const int st = solve_with_warm_start(ctx, b, phi, width, height, ld, o, stats, j.work);
+    PCD_TRY(j.end());
+    return st;
 }
 
 int pcd_poisson_solve(pcd_ctx *ctx, const double *b, double *phi, int width, int height,
@@ -158,8 +216,9 @@ int pcd_poisson_solve(pcd_ctx *ctx, const double *b, double *phi, int width, int
     PCD_TRY(ctx_stage(ctx, n));
     cudaStream_t s = ctx->stream;
     PCD_CUDA(cudaMemcpyAsync(ctx->d_b, b, n * sizeof(double), cudaMemcpyHostToDevice, s));
-    if (o.warm_start) PCD_CUDA(cudaMemcpyAsync(ctx->d_phi, phi, n * sizeof(double), cudaMemcpyHostToDevice, s));
-    int st = solve_device(ctx->solver, ctx->d_b, ctx->d_phi, width, height, width, o, stats, s);
+    if (o.warm_start == PCD_WARM_GIVEN)
+        PCD_CUDA(cudaMemcpyAsync(ctx->d_phi, phi, n * sizeof(double), cudaMemcpyHostToDevice, s));
+    int st = solve_with_warm_start(ctx, ctx->d_b, ctx->d_phi, width, height, width, o, stats, s);
     if (st != PCD_OK && st != PCD_NOT_CONVERGED) return st;
     PCD_CUDA(cudaMemcpyAsync(phi, ctx->d_phi, n * sizeof(double), cudaMemcpyDeviceToHost, s));
     PCD_CUDA(cudaStreamSynchronize(s));
@@ -216,8 +275,11 @@ int pcd_batch_solve_device(pcd_ctx *ctx, const pcd_instance *inst, int count, co
         o.stop = PCD_STOP_REL_RESIDUAL;
         o.tol = 1e-6;
     }
-    return batch_solve_device(ctx->batch, ctx->device, inst, count, o, stats, batch_stats,
-                              stream ? (cudaStream_t)stream : ctx->stream);
+    StreamJoin j(ctx, stream);
+    PCD_TRY(j.begin());
+    const int st = batch_solve_device(ctx->batch, ctx->device, inst, count, o, stats, batch_stats, j.work);
+    PCD_TRY(j.end());
+    return st;
 }
 
 int pcd_subtract_average_device(pcd_ctx *ctx, double *g, int width, int height, void *stream)
@@ -225,7 +287,10 @@ int pcd_subtract_average_device(pcd_ctx *ctx, double *g, int width, int height, 
     if (!ctx || !g || width < 1 || height < 1) return PCD_BAD_ARG;
     std::lock_guard<std::mutex> lk(ctx->mu);
     PCD_TRY(ctx_activate(ctx));
-    return subtract_average(ctx->grid, g, (long)width * height, stream ? (cudaStream_t)stream : ctx->stream);
+    StreamJoin j(ctx, stream);
+    PCD_TRY(j.begin());
+    PCD_TRY(subtract_average(ctx->grid, g, (long)width * height, j.work));
+    return j.end();
 }
 
 int pcd_gradient_device(pcd_ctx *ctx, const double *g, double *gx, double *gy, int width, int height,
@@ -234,7 +299,10 @@ int pcd_gradient_device(pcd_ctx *ctx, const double *g, double *gx, double *gy, i
     if (!ctx || !g || !gx || !gy || width < 1 || height < 1) return PCD_BAD_ARG;
     std::lock_guard<std::mutex> lk(ctx->mu);
     PCD_TRY(ctx_activate(ctx));
-    return gradient(g, gx, gy, width, height, stream ? (cudaStream_t)stream : ctx->stream);
+    StreamJoin j(ctx, stream);
+    PCD_TRY(j.begin());
+    PCD_TRY(gradient(g, gx, gy, width, height, j.work));
+    return j.end();
 }
 
 int pcd_divergence_device(pcd_ctx *ctx, const double *nx, const double *ny, double *div, int width, int height,
@@ -243,7 +311,10 @@ int pcd_divergence_device(pcd_ctx *ctx, const double *nx, const double *ny, doub
     if (!ctx || !nx || !ny || !div || width < 1 || height < 1) return PCD_BAD_ARG;
     std::lock_guard<std::mutex> lk(ctx->mu);
     PCD_TRY(ctx_activate(ctx));
-    return divergence(nx, ny, div, width, height, stream ? (cudaStream_t)stream : ctx->stream);
+    StreamJoin j(ctx, stream);
+    PCD_TRY(j.begin());
+    PCD_TRY(divergence(nx, ny, div, width, height, j.work));
+    return j.end();
 }
 
 }  // extern "C"

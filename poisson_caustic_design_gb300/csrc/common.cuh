@@ -37,6 +37,13 @@ void count_launches(unsigned long long n);
         ::pcd::count_launches(n);                                                          \
     } while (0)
 
+__device__ __forceinline__ float warp_sum_f(float v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
 __device__ __forceinline__ double warp_sum(double v)
 {
 #pragma unroll

@@ -1,0 +1,57 @@
+// nn.cuh -- kernels of the learned warm start (internal).
+#pragma once
+
+#include <cuda_bf16.h>
+
+#include "common.cuh"
+
+namespace pcd {
+namespace nn {
+
+struct GemmArgs {
+    const __nv_bfloat16 *A;  // M x K, row stride lda
+    int lda;
+    const __nv_bfloat16 *B;  // N x K, row stride ldb
+    int ldb;
+    int M, N, K;             // K multiple of 32
+    int ksplit;              // K splits (partials reduced in a fixed order)
+    const float *bias;       // [N] or null
+    int relu;
+    __nv_bfloat16 *Cb;       // BF16 output (row stride ldc), or
+    float *Cf;               // FP32 output
+    int ldc;
+};
+
+struct AdamParams {
+    float lr, beta1, beta2, eps, wd;
+};
+
+size_t gemm_smem(int BN);
+// partials: ksplit * M * N floats when ksplit > 1
+int gemm(const GemmArgs &g, cudaStream_t s, float *partials);
+int im2col(const __nv_bfloat16 *in, int B, int H, int W, int C, int ldcin, __nv_bfloat16 *out, int Kp, cudaStream_t s);
+int transpose(const __nv_bfloat16 *in, int rows, int cols, int ldin, __nv_bfloat16 *out, int ldout, cudaStream_t s);
+int flip(const __nv_bfloat16 *Wt, int Cout, int Cin, int Kp, __nv_bfloat16 *Wf, int Kpf, cudaStream_t s);
+int relu_bwd(const float *dY, int lddy, const __nv_bfloat16 *Y, int ldy, long P, int C, int relu, __nv_bfloat16 *dYm,
+             cudaStream_t s);
+int colsum(const __nv_bfloat16 *X, long P, int C, float *part, float *out, cudaStream_t s);
+// out[c] = sum over rows of part[r][c] (FP32, fixed order)
+int colsum_f32(const float *part, int rows, int C, float *out, cudaStream_t s);
+int pool(const __nv_bfloat16 *in, int B, int H, int W, int C, int ldin, __nv_bfloat16 *out, cudaStream_t s);
+int pool_bwd(const float *dOut, int B, int H, int W, int C, float *dIn, int lddin, cudaStream_t s);
+int up(const __nv_bfloat16 *in, int B, int H, int W, int C, __nv_bfloat16 *out, int ldout, cudaStream_t s);
+int up_bwd(const float *dOut, int lddout, int B, int H, int W, int C, float *dIn, cudaStream_t s);
+int head(const __nv_bfloat16 *X, long P, int C, const float *w, const float *bias, float *out, cudaStream_t s);
+int head_bwd(const float *d, const __nv_bfloat16 *X, long P, int C, const float *w, float *dX, float *part,
+             int *nparts, cudaStream_t s);
+int mse(const float *pred, const float *tgt, long P1, int B, float *means, float *d, float *loss_part, int *nparts,
+        cudaStream_t s);
+int adamw(float *w, const float *grad, float *m, float *v, long n, int cols, int ld, const AdamParams &p, int step,
+          __nv_bfloat16 *wb, cudaStream_t s);
+int f32_to_bf16(const float *x, long n, __nv_bfloat16 *y, cudaStream_t s);
+int bf16_to_f32(const __nv_bfloat16 *x, long n, float *y, int ldx, int cols, cudaStream_t s);
+int fill(float *x, long n, float v, cudaStream_t s);
+int slice_add(const float *in, long P, int C, float *out, int ld, int accumulate, cudaStream_t s);
+
+}  // namespace nn
+}  // namespace pcd

@@ -792,6 +792,32 @@ int solve_cluster(SolverWorkspace &ws, const double *b, double *phi, const Solve
 
 }  // namespace
 
+int residual_rel(SolverWorkspace &ws, const double *b, const double *phi, int W, int H, int ld, cudaStream_t s,
+                 double *rel)
+{
+    PCD_TRY(ws.reserve((size_t)H * ld));
+    SolveArgs a{};
+    a.W = W; a.H = H; a.ld = ld;
+    a.stop = PCD_STOP_REL_RESIDUAL;
+    PCD_CUDA(cudaMemsetAsync(ws.ctl, 0, sizeof(Ctl), s));
+    const int rblocks = grid_blocks((long)W * H);
+    k_mask<<<rblocks, kThreads, 0, s>>>(b, ws.mask, W, H, ld, ws.ctl);
+    PCD_LAUNCHED(1);
+    k_residual64<true><<<rblocks, kThreads, 0, s>>>(phi, b, ws.mask, ws.ctl, ws.partials, a, 0, 1, 0);
+    PCD_LAUNCHED(1);
+    PCD_CUDA(cudaMemcpyAsync(ws.ctl_host, ws.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, s));
+    PCD_CUDA(cudaStreamSynchronize(s));
+    *rel = ws.ctl_host[0].rel;
+    return PCD_OK;
+}
+
+int zero_grid(double *phi, int W, int H, int ld, cudaStream_t s)
+{
+    k_fill<<<grid_blocks((long)W * H), kThreads, 0, s>>>(phi, W, H, ld, 0.0);
+    PCD_LAUNCHED(1);
+    return PCD_OK;
+}
+
 int solve_device(SolverWorkspace &ws, const double *b, double *phi, int W, int H, int ld, const pcd_solve_opts &o,
                  pcd_solve_stats *stats, cudaStream_t s)
 {

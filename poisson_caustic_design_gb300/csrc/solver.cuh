@@ -81,6 +81,11 @@ struct SolverWorkspace {
     void release();
 };
 
+// ||b - L phi|| / ||b|| (FP64) of a given phi
+int residual_rel(SolverWorkspace &ws, const double *b, const double *phi, int W, int H, int ld, cudaStream_t s,
+                 double *rel);
+int zero_grid(double *phi, int W, int H, int ld, cudaStream_t s);
+
 int solve_device(SolverWorkspace &ws, const double *b, double *phi, int W, int H, int ld,
                  const pcd_solve_opts &o, pcd_solve_stats *stats, cudaStream_t s);
 

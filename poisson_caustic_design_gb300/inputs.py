@@ -84,3 +84,39 @@ def poisson_rhs(n: int, seed: int = 0, kind: str = "gaussian", m: int | None = N
     b -= b.mean()
     b -= b.mean()
     return np.ascontiguousarray(b)
+
+
+def poisson_rhs_torch(n: int, seeds, device="cuda"):
+    """Batched GPU version of ``poisson_rhs`` for training data: for each seed
+    the same parameters are drawn (Gaussian mixture for even seeds, binary
+    shapes for odd seeds) and the fields are evaluated with torch in FP64.
+    Returns an [len(seeds), n, n] float64 tensor of mean-free right-hand sides."""
+    import torch
+
+    y = (torch.arange(n, device=device, dtype=torch.float64) + 0.5) / n
+    Y, X = torch.meshgrid(y, y, indexing="ij")
+    out = []
+    for s in seeds:
+        rng = np.random.default_rng(s)
+        if s % 2 == 0:
+            rho = torch.full((n, n), 0.05, device=device, dtype=torch.float64)
+            for _ in range(16):
+                cx, cy = rng.uniform(0.1, 0.9, size=2)
+                sg = rng.uniform(0.03, 0.15)
+                a = rng.uniform(0.2, 1.0)
+                rho += a * torch.exp(-((X - cx) ** 2 + (Y - cy) ** 2) / (2 * sg * sg))
+        else:
+            rho = torch.full((n, n), 0.02, device=device, dtype=torch.float64)
+            for _ in range(20):
+                cx, cy = rng.uniform(0.05, 0.95, size=2)
+                if rng.uniform() < 0.5:
+                    r = rng.uniform(0.03, 0.15)
+                    rho[(X - cx) ** 2 + (Y - cy) ** 2 <= r * r] = 1.0
+                else:
+                    hw, hh = rng.uniform(0.03, 0.15, size=2)
+                    rho[((X - cx).abs() <= hw) & ((Y - cy).abs() <= hh)] = 1.0
+        b = rho / rho.mean() - 1.0
+        b = b - b.mean()
+        b = b - b.mean()
+        out.append(b)
+    return torch.stack(out)

@@ -41,7 +41,7 @@ class SolveOptions:
     omega: float = 0.0
     check_every: int = 0
     refine_every: int = 0
-    warm_start: bool = True
+    warm_start: int = 1      # 0 zero, 1 phi is the initial guess, 2 learned prediction
     schedule: int = 0
 
     def to_c(self) -> _lib.SolveOpts:
@@ -53,7 +53,7 @@ class SolveOptions:
         o.omega = float(self.omega)
         o.check_every = int(self.check_every)
         o.refine_every = int(self.refine_every)
-        o.warm_start = 1 if self.warm_start else 0
+        o.warm_start = int(self.warm_start)
         o.schedule = int(self.schedule)
         return o
 

@@ -1,0 +1,199 @@
+"""The learned warm start: the tensor-core GEMM against torch, the U-Net's
+forward pass and gradients against a float32 torch CPU model of the same
+network (autograd as the gradient oracle), a short training run, and the
+warm-start policy inside the solve (prediction kept only when it beats a zero
+guess)."""
+import os
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("M,N,K,ksplit", [(200, 96, 64, 1), (130, 32, 288, 1), (64, 250, 96, 1), (256, 128, 4096, 8),
+                                          (33, 700, 160, 3)])
+def test_gemm_matches_torch(M, N, K, ksplit):
+    import torch
+
+    from poisson_caustic_design_gb300 import _lib
+
+    L = _lib.load()
+    g = torch.Generator(device="cpu").manual_seed(M + N + K)
+    A = torch.randn(M, K, generator=g).to(torch.bfloat16).cuda()
+    B = torch.randn(N, K, generator=g).to(torch.bfloat16).cuda()
+    C = torch.zeros(M, N, dtype=torch.float32, device="cuda")
+    part = torch.zeros(ksplit * M * N, dtype=torch.float32, device="cuda")
+    st = L.pcd_gemm_bf16(A.data_ptr(), K, B.data_ptr(), K, C.data_ptr(), N, M, N, K, ksplit, part.data_ptr(),
+                         torch.cuda.current_stream().cuda_stream)
+    assert st == 0, L.pcd_last_error()
+    torch.cuda.synchronize()
+    ref = A.float() @ B.float().T
+    err = (C - ref).abs().max().item() / ref.abs().max().item()
+    assert err < 1e-5, err
+
+
+def torch_unet(params, x, bf16=False):
+    """float32 CPU model of the library's U-Net with the flat parameters.
+
+    With ``bf16`` the model rounds where the library stores BF16: conv inputs
+    and weights (forward only) and every conv output, whose incoming gradient
+    is rounded too (the library converts dY to BF16 before its GEMMs)."""
+    import torch
+    import torch.nn.functional as F
+
+    from poisson_caustic_design_gb300 import learned
+
+    layout, _ = learned.param_layout()
+    P = {name: torch.tensor(params[off:off + int(np.prod(shape))].reshape(shape), requires_grad=True)
+         for name, off, shape in layout}
+
+    class RoundBoth(torch.autograd.Function):
+        @staticmethod
+        def forward(ctx, t):
+            return t.bfloat16().float()
+
+        @staticmethod
+        def backward(ctx, g):
+            return g.bfloat16().float()
+
+    ident = lambda t: t
+    fwd = (lambda t: t + (t.bfloat16().float() - t).detach()) if bf16 else ident
+    both = RoundBoth.apply if bf16 else ident
+
+    def conv(i, h):
+        ci, co, _ = learned.LAYERS[i]
+        w = P[f"conv{i}.w"][:, :9 * ci].reshape(co, 3, 3, ci).permute(0, 3, 1, 2)
+        return both(F.relu(F.conv2d(fwd(h), fwd(w), P[f"conv{i}.b"], padding=1)))
+
+    up = lambda h: F.interpolate(h, scale_factor=2, mode="nearest")
+    pool = lambda h: F.avg_pool2d(h, 2)
+    s1 = conv(1, conv(0, x))
+    s2 = conv(3, conv(2, pool(s1)))
+    s3 = conv(5, conv(4, pool(s2)))
+    u4 = conv(7, conv(6, pool(s3)))
+    u3 = conv(9, conv(8, torch.cat([up(u4), s3], 1)))
+    u2 = conv(11, conv(10, torch.cat([up(u3), s2], 1)))
+    u1 = conv(13, conv(12, torch.cat([up(u2), s1], 1)))
+    out = F.conv2d(u1, P["head.w"].reshape(1, 32, 1, 1), P["head.b"])
+    return out[:, 0], P
+
+
+def _torch_loss_grads(params, xn, tg, bf16):
+    import torch
+
+    ref, P = torch_unet(params, xn[:, None], bf16)
+    tt = torch.from_numpy(tg)
+    d = (ref - ref.mean(dim=(1, 2), keepdim=True)) - (tt - tt.mean(dim=(1, 2), keepdim=True))
+    lref = (d ** 2).mean()
+    lref.backward()
+    return ref.detach().numpy(), lref.item(), {k: v.grad.numpy().ravel() for k, v in P.items()}
+
+
+def test_unet_forward_and_gradients_match_torch(ctx):
+    """Forward, loss and parameter gradients of one training step against
+    autograd.  The gradient oracle is the model with BF16 rounding at the
+    library's storage points; the FP32 model is a looser cross-check (BF16
+    rounding alone moves the deepest layers' gradients by ~10% relative from
+    FP32 on this random-init network).  head.b is skipped: the loss is
+    invariant to a constant shift of the prediction, so its gradient is zero
+    up to rounding."""
+    import torch
+
+    from poisson_caustic_design_gb300 import inputs, learned
+
+    S, B = 32, 2
+    net = learned.UNet(ctx, resolution=S, max_batch=B, seed=3)
+    params = net.get_params()
+    bs = np.stack([inputs.poisson_rhs(S, 5 + i, "gaussian") for i in range(B)]).astype(np.float32)
+    tg = np.stack([np.sin(np.linspace(0, 3, S * S)).reshape(S, S) * (i + 1) for i in range(B)]).astype(np.float32)
+    x = torch.from_numpy(bs).cuda()
+    t = torch.from_numpy(tg).cuda()
+    pred = net.predict(x).cpu().numpy()
+    # the model normalises each sample: (b - mean) / std
+    xn = torch.from_numpy((bs - bs.mean(axis=(1, 2), keepdims=True)) / bs.std(axis=(1, 2), keepdims=True))
+    r32, l32, g32 = _torch_loss_grads(params, xn, tg, bf16=False)
+    r16, l16, g16 = _torch_loss_grads(params, xn, tg, bf16=True)
+    assert np.linalg.norm(pred - r16) / np.linalg.norm(r16) < 2e-2
+    assert np.linalg.norm(pred - r32) / np.linalg.norm(r32) < 3e-2
+    # gradients of one training step (lr = 0 leaves the weights unchanged)
+    loss = net.train_step(x, t, lr=0.0)
+    assert abs(loss - l16) <= 2e-2 * l16 and abs(loss - l32) <= 3e-2 * l32
+    g = net.grads()
+    layout, _ = learned.param_layout()
+    for name, off, shape in layout:
+        if name == "head.b":
+            continue
+        go = g[off:off + g16[name].size]
+        for gt, rel_tol, cos_tol in ((g16[name], 0.06, 0.998), (g32[name], 0.15, 0.99)):
+            nt = np.linalg.norm(gt)
+            rel = np.linalg.norm(go - gt) / nt
+            cos = float(go @ gt / (np.linalg.norm(go) * nt + 1e-30))
+            assert rel < rel_tol and cos > cos_tol, (name, rel, cos)
+    net.close()
+
+
+def test_training_reduces_loss(ctx):
+    import torch
+
+    from poisson_caustic_design_gb300 import learned
+
+    S = 64
+    net = learned.UNet(ctx, resolution=S, max_batch=8, seed=1)
+    x, t = learned.make_pairs(ctx, range(16), S, tol=1e-6)
+    hist = learned.train(net, x, t, epochs=40, batch=8, lr=3e-3)
+    assert hist[-1] < 0.3 * hist[0], hist
+    net.close()
+
+
+def test_learned_warm_start_policy(ctx):
+    """An untrained network's prediction is rejected unless it beats a zero
+    guess; either way the solve reaches the tolerance."""
+    import torch
+
+    import poisson_caustic_design_gb300 as pcd
+    from poisson_caustic_design_gb300 import learned
+
+    net = learned.UNet(ctx, resolution=64, max_batch=1, seed=7)
+    net.attach(ctx)
+    b = torch.from_numpy(pcd.inputs.poisson_rhs(128, 3, "gaussian")).cuda()
+    phi = torch.zeros_like(b)
+    st = ctx.solve_device(b, phi, pcd.SolveOptions(stop=pcd.STOP_REL_RESIDUAL, tol=1e-6, precision=pcd.PREC_MIXED,
+                                                   omega=-1.0, warm_start=2))
+    assert st["converged"] == 1 and st["warm_used"] in (2, 3)
+    assert (st["warm_used"] == 2) == (st["warm_rel_residual"] < 1.0)
+    pcd_ctx_clear = pcd._lib.load().pcd_ctx_set_warm_start_net(ctx.handle, None)
+    assert pcd_ctx_clear == 0
+    with pytest.raises(pcd.PCDError):
+        ctx.solve_device(b, phi, pcd.SolveOptions(stop=pcd.STOP_REL_RESIDUAL, tol=1e-6, warm_start=2))
+    net.close()
+
+
+def test_trained_network_gains_over_zero_guess(ctx):
+    """With the committed trained weights the learned warm start is accepted
+    and needs fewer sweeps than the zero guess on held-out 256^2 and 512^2
+    densities."""
+    import torch
+
+    import poisson_caustic_design_gb300 as pcd
+    from poisson_caustic_design_gb300 import learned
+
+    path = learned.default_weights_path(256)
+    if not os.path.exists(path):
+        pytest.skip("no trained weights in this checkout")
+    net = learned.UNet(ctx, resolution=256, max_batch=1)
+    net.load(path)
+    net.attach(ctx)
+    for n, seed in ((256, 900001), (512, 900002), (256, 900003)):
+        b = torch.from_numpy(pcd.inputs.poisson_rhs(n, seed, "gaussian" if seed % 2 else "binary")).cuda()
+        sweeps = {}
+        for warm in (0, 2):
+            phi = torch.zeros_like(b)
+            st = ctx.solve_device(b, phi, pcd.SolveOptions(stop=pcd.STOP_REL_RESIDUAL, tol=1e-6,
+                                                           precision=pcd.PREC_MIXED, omega=-1.0, warm_start=warm))
+            assert st["converged"]
+            sweeps[warm] = st["sweeps"]
+            if warm == 2:
+                assert st["warm_used"] == 2 and st["warm_rel_residual"] < 1.0
+        assert sweeps[2] < sweeps[0], sweeps
+    net.close()
