@@ -362,22 +362,24 @@ def run_ours(args, rank, world, local, pg):
                    "clusters": bst["clusters"], "cluster_size": bst["cluster_size"]}
         del bb, pp
 
-    # HBM-bound sweep roofline: fused red+black stripe sweeps on 4096^2 (FP32
-    # 12 B and FP64 24 B algorithmic per cell-sweep), 256 sweeps per solve
+    # HBM-bound sweep roofline on 4096^2, 256 sweeps per solve: FP32 stream
+    # sweeps (12 B algorithmic per cell-sweep), FP64 in-place stripes (24 B)
     stream_roof = None
     if not args.no_batch:
         n4 = 4096
         b4 = pcd.inputs.poisson_rhs_torch(n4, [77])[0].contiguous()
         p4 = torch.zeros_like(b4)
         stream_roof = {}
-        for prec, bpc, nm in ((pcd.PREC_MIXED, 12, "fp32_sweeps"), (pcd.PREC_FP64, 24, "fp64_sweeps")):
+        for prec, bpc, nm, sch in ((pcd.PREC_MIXED, 12, "fp32_sweeps", pcd.SCHED_STREAM),
+                                   (pcd.PREC_FP64, 24, "fp64_sweeps", pcd.SCHED_STRIPES)):
             o4 = pcd.SolveOptions(stop=pcd.STOP_REL_RESIDUAL, tol=0.0, max_iterations=256, omega=-1.0, precision=prec,
-                                  warm_start=0, schedule=pcd.SCHED_STRIPES, refine_every=256)
+                                  warm_start=0, schedule=sch, refine_every=256)
             ctx.solve_device(b4, p4, o4, stream=stream.cuda_stream)
             st4 = ctx.solve_device(b4, p4, o4, stream=stream.cuda_stream)
             per_sweep = st4["sweep_ms"] * 1e-3 / st4["sweeps"]
             ach = bpc * n4 * n4 / per_sweep / 1e9
-            stream_roof[nm] = {"us_per_sweep": per_sweep * 1e6, "achieved_gbs": ach, "frac_hbm": ach / peak}
+            stream_roof[nm] = {"us_per_sweep": per_sweep * 1e6, "achieved_gbs": ach, "frac_hbm": ach / peak,
+                               "schedule": int(st4["schedule_used"])}
         del b4, p4
 
     cpu = None

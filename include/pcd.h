@@ -93,9 +93,15 @@ typedef enum {
     PCD_SCHED_CLUSTER = 3,     /* mixed precision with the relative-residual stop: FP32 sweeps
                                   on one 16-CTA cluster (grid fits in its shared memory),
                                   FP64 defect correction on all SMs between cycles */
-    PCD_SCHED_STRIPES = 4      /* grids in HBM without NaN cells: one fused red+black pass per
-                                  sweep (row stripes walked top-down), CUDA-graph chunks; AUTO
-                                  picks it when the on-chip schedules do not fit */
+    PCD_SCHED_STRIPES = 4,     /* grids in HBM without NaN cells: one fused red+black pass per
+                                  sweep (row stripes walked top-down, in place), CUDA-graph
+                                  chunks; AUTO picks it for FP64 sweeps when the on-chip
+                                  schedules do not fit */
+    PCD_SCHED_STREAM = 5       /* mixed precision, grids in HBM without NaN cells, ld a multiple
+                                  of 4, W <= 4096: one pass per sweep from one FP32 correction
+                                  buffer into another (row window in registers, stripe edges
+                                  recomputed, no boundary pass); AUTO picks it for FP32 sweeps
+                                  when the on-chip schedules do not fit */
 } pcd_schedule;
 
 typedef struct {

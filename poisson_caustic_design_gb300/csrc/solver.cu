@@ -438,6 +438,73 @@ inline int stripe_rows(int H, int resident)
     return R < 3 ? 3 : R;
 }
 
+#include "sor_stream.cuh"
+
+// Launch shape of the ping-pong stream sweep: G 4-cell groups per thread,
+// T threads (one row of the grid per block), ns stripes of R rows; rows
+// staged by bulk copies (tma, rows of wpad floats, smem bytes of dynamic
+// shared memory) or loaded into registers.
+struct StreamPlan {
+    int G = 0, T = 0, R = 0, ns = 0;
+    int tma = 0, wpad = 0;
+    size_t smem = 0;
+};
+
+int stream_plan(int dev, int W, int H, int ld, bool allow_tma, StreamPlan *p)
+{
+    const int groups = (W + 3) / 4;
+    // two groups per thread at most: four would not fit in 128 registers
+    if (H < 3 || ld % 4 != 0 || groups > 2 * kStreamThreadsMax) return PCD_BAD_ARG;
+    const int G = groups <= kStreamThreadsMax ? 1 : 2;
+    const int T = 32 * ceil_div(ceil_div(groups, G), 32);
+    int sms = 0, bps = 0, max_smem = 0;
+    PCD_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    PCD_CUDA(cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    const int wpad = 4 * groups;
+    const size_t smem = tma_smem_bytes(wpad);
+    const bool tma = allow_tma && smem <= (size_t)max_smem;
+    if (tma) {
+        const void *fn = G == 1 ? (const void *)k_sweep_tma<1> : (const void *)k_sweep_tma<2>;
+        PCD_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        PCD_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, fn, T, smem));
+    } else if (G == 1) {
+        PCD_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_sweep_stream<1, false>, T, 0));
+    } else {
+        PCD_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_sweep_stream<2, false>, T, 0));
+    }
+    if (bps < 1) return PCD_BAD_ARG;
+    int ns = std::min(bps * sms, ceil_div(H, kStreamRowsMin));
+    if (ns < 1) ns = 1;
+    const int R = ceil_div(H, ns);
+    p->G = G;
+    p->T = T;
+    p->R = R;
+    p->ns = ceil_div(H, R);
+    p->tma = tma ? 1 : 0;
+    p->wpad = wpad;
+    p->smem = tma ? smem : 0;
+    return PCD_OK;
+}
+
+constexpr long kTmaSpinLimit = 1l << 22;
+
+template <bool TRACK>
+void launch_stream_t(const StreamPlan &p, const float *ein, float *eout, const float *r, Ctl *ctl, const SolveArgs &a,
+                     int out_idx, cudaStream_t s)
+{
+    if (p.tma && !TRACK) {
+        if (p.G == 1)
+            k_sweep_tma<1><<<p.ns, p.T, p.smem, s>>>(ein, eout, r, ctl, a, p.R, out_idx, p.wpad, kTmaSpinLimit);
+        else
+            k_sweep_tma<2><<<p.ns, p.T, p.smem, s>>>(ein, eout, r, ctl, a, p.R, out_idx, p.wpad, kTmaSpinLimit);
+    } else if (p.G == 1) {
+        k_sweep_stream<1, TRACK><<<p.ns, p.T, 0, s>>>(ein, eout, r, ctl, a, p.R, out_idx);
+    } else {
+        k_sweep_stream<2, TRACK><<<p.ns, p.T, 0, s>>>(ein, eout, r, ctl, a, p.R, out_idx);
+    }
+}
+
+
 __global__ void k_fill(double *p, int W, int H, int ld, double v)
 {
     const long n = (long)W * H;
@@ -477,13 +544,15 @@ int SolverWorkspace::reserve(size_t n)
     if (n > cells) {
         if (mask) cudaFree(mask);
         if (e32) cudaFree(e32);
+        if (e32b) cudaFree(e32b);
         if (r32) cudaFree(r32);
         if (r64) cudaFree(r64);
-        mask = nullptr; e32 = nullptr; r32 = nullptr; r64 = nullptr;
+        mask = nullptr; e32 = nullptr; e32b = nullptr; r32 = nullptr; r64 = nullptr;
         for (auto &kv : graphs) cudaGraphExecDestroy(kv.second.exec);
         graphs.clear();
         PCD_CUDA(cudaMalloc(&mask, n));
         PCD_CUDA(cudaMalloc(&e32, n * sizeof(float)));
+        PCD_CUDA(cudaMalloc(&e32b, n * sizeof(float)));
         PCD_CUDA(cudaMalloc(&r32, n * sizeof(float)));
         PCD_CUDA(cudaMalloc(&r64, n * sizeof(double)));
         cells = n;
@@ -497,6 +566,7 @@ void SolverWorkspace::release()
     graphs.clear();
     if (mask) cudaFree(mask);
     if (e32) cudaFree(e32);
+    if (e32b) cudaFree(e32b);
     if (r32) cudaFree(r32);
     if (r64) cudaFree(r64);
     if (xbuf) cudaFree(xbuf);
@@ -513,7 +583,8 @@ void SolverWorkspace::release()
     if (t1) cudaEventDestroy(t1);
     if (k0) cudaEventDestroy(k0);
     if (k1) cudaEventDestroy(k1);
-    mask = nullptr; e32 = nullptr; r32 = nullptr; partials = nullptr; ctl = nullptr; ctl_host = nullptr;
+    mask = nullptr; e32 = nullptr; e32b = nullptr; r32 = nullptr; partials = nullptr; ctl = nullptr;
+    ctl_host = nullptr;
     cells = 0;
 }
 
@@ -540,8 +611,9 @@ int launch_stripes(T *phi, const T *rhs, Ctl *ctl, const SolveArgs &a, int R, in
 // Enqueues one chunk of `sweeps` sweeps (plus the checks that follow them) on s.
 template <bool MASKED>
 int enqueue_chunk(SolverWorkspace &ws, const double *b, double *phi, const SolveArgs &a, int precision,
-                  int sweeps, cudaStream_t s, int *nodes, bool stripes)
+                  int sweeps, cudaStream_t s, int *nodes, int sched, const StreamPlan &sp)
 {
+    const bool stripes = sched == PCD_SCHED_STRIPES;
     const int half = (a.W + 1) >> 1;
     const int blocks = ceil_div((long)a.H * half, kThreads);
     const int rblocks = grid_blocks((long)a.W * a.H);
@@ -562,6 +634,20 @@ int enqueue_chunk(SolverWorkspace &ws, const double *b, double *phi, const Solve
             }
             n += 2;
         }
+        sweeps = 0;
+    }
+    if (!MASKED && sched == PCD_SCHED_STREAM) {
+        // sweep k reads buffer k&1 and writes the other; the settle kernel
+        // moves the latest correction into e32 for the refinement
+        for (int k = 0; k < sweeps; k++) {
+            const float *ein = (k & 1) ? ws.e32b : ws.e32;
+            float *eout = (k & 1) ? ws.e32 : ws.e32b;
+            if (track) launch_stream_t<true>(sp, ein, eout, ws.r32, ws.ctl, a, (k & 1) ? 0 : 1, s);
+            else launch_stream_t<false>(sp, ein, eout, ws.r32, ws.ctl, a, (k & 1) ? 0 : 1, s);
+            n++;
+        }
+        k_stream_settle<<<rblocks, kThreads, 0, s>>>(ws.e32, ws.e32b, ws.ctl, a);
+        n++;
         sweeps = 0;
     }
     for (int k = 0; k < sweeps; k++) {
@@ -595,10 +681,11 @@ int enqueue_chunk(SolverWorkspace &ws, const double *b, double *phi, const Solve
 }
 
 int get_chunk_graph(SolverWorkspace &ws, const double *b, double *phi, const SolveArgs &a, int precision,
-                    int masked, int sweeps, cudaStream_t s, SolverWorkspace::GraphEntry **out, bool stripes)
+                    int masked, int sweeps, cudaStream_t s, SolverWorkspace::GraphEntry **out, int sched,
+                    const StreamPlan &sp)
 {
     std::vector<long long> key = {(long long)(uintptr_t)b, (long long)(uintptr_t)phi, a.W, a.H, a.ld, a.stop,
-                                  a.max_iter, precision, masked, sweeps, stripes ? 1 : 0};
+                                  a.max_iter, precision, masked, sweeps, sched, sp.G, sp.T, sp.R, sp.tma};
     long long tb, ob;
     std::memcpy(&tb, &a.tol, 8);
     std::memcpy(&ob, &a.omega, 8);
@@ -612,8 +699,8 @@ int get_chunk_graph(SolverWorkspace &ws, const double *b, double *phi, const Sol
     cudaGraph_t g;
     int nodes = 0;
     PCD_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-    int st = masked ? enqueue_chunk<true>(ws, b, phi, a, precision, sweeps, s, &nodes, false)
-                    : enqueue_chunk<false>(ws, b, phi, a, precision, sweeps, s, &nodes, stripes);
+    int st = masked ? enqueue_chunk<true>(ws, b, phi, a, precision, sweeps, s, &nodes, PCD_SCHED_LAUNCHES, sp)
+                    : enqueue_chunk<false>(ws, b, phi, a, precision, sweeps, s, &nodes, sched, sp);
     cudaError_t ce = cudaStreamEndCapture(s, &g);
     if (st != PCD_OK) return st;
     if (ce != cudaSuccess) {
@@ -892,9 +979,18 @@ int solve_device(SolverWorkspace &ws, const double *b, double *phi, int W, int H
         PCD_LAUNCHED(1);
     }
 
-    // fused stripe sweeps for grids with at least 3 rows and no NaN cells
-    const bool stripes = !masked && H >= 3 && W <= 2 * kRowCellsMax * kStripeThreads &&
-                         o.schedule != PCD_SCHED_LAUNCHES;
+    // HBM grids without NaN cells: ping-pong stream sweeps (FP32), else fused
+    // in-place stripe sweeps (grids with at least 3 rows)
+    int sched = PCD_SCHED_LAUNCHES;
+    StreamPlan sp;
+    if (!masked && precision == PCD_PREC_MIXED &&
+        (o.schedule == PCD_SCHED_AUTO || o.schedule == PCD_SCHED_STREAM || o.schedule == PCD_SCHED_PERSISTENT ||
+         o.schedule == PCD_SCHED_CLUSTER) &&
+        stream_plan(ws.dev, W, H, ld, a.stop == PCD_STOP_REL_RESIDUAL, &sp) == PCD_OK)
+        sched = PCD_SCHED_STREAM;
+    else if (!masked && H >= 3 && W <= 2 * kRowCellsMax * kStripeThreads && o.schedule != PCD_SCHED_LAUNCHES)
+        sched = PCD_SCHED_STRIPES;
+    const bool stripes = sched == PCD_SCHED_STRIPES;
     if (stripes && ws.stripe_resident == 0) {
         int sms = 0, bps = 0;
         PCD_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ws.dev));
@@ -915,7 +1011,7 @@ int solve_device(SolverWorkspace &ws, const double *b, double *phi, int W, int H
     if (chunk > a.max_iter && a.max_iter > 0) chunk = a.max_iter;
 
     SolverWorkspace::GraphEntry *ge = nullptr;
-    if (!done_already) PCD_TRY(get_chunk_graph(ws, b, phi, a, precision, masked, chunk, s, &ge, stripes));
+    if (!done_already) PCD_TRY(get_chunk_graph(ws, b, phi, a, precision, masked, chunk, s, &ge, sched, sp));
 
     PCD_CUDA(cudaEventRecord(ws.k0, s));
     // Chunk loop: launch chunk i+1 before inspecting chunk i's control block.
@@ -953,6 +1049,10 @@ int solve_device(SolverWorkspace &ws, const double *b, double *phi, int W, int H
     PCD_CUDA(cudaMemcpyAsync(&ws.ctl_host[0], ws.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, s));
     PCD_CUDA(cudaStreamSynchronize(s));
     const Ctl &c = ws.ctl_host[0];
+    if (c.error) {
+        set_error("stream SOR: a bounded wait for a row copy gave up (status " + std::to_string(c.error) + ")");
+        return c.error;
+    }
     if (stats) {
         stats->sweeps = c.sweeps;
         stats->converged = c.converged;
@@ -965,7 +1065,7 @@ int solve_device(SolverWorkspace &ws, const double *b, double *phi, int W, int H
         stats->device_ms = ms;
         cudaEventElapsedTime(&ms, ws.k0, ws.k1);
         stats->sweep_ms = ms;
-        stats->schedule_used = stripes ? PCD_SCHED_STRIPES : PCD_SCHED_LAUNCHES;
+        stats->schedule_used = sched;
     }
     return c.converged ? PCD_OK : PCD_NOT_CONVERGED;
 }

@@ -27,7 +27,7 @@ struct Ctl {
     int checks;                  // residual evaluations
     int nan_cells;               // NaN entries of b
     int error;                   // PCD_TIMEOUT when a bounded device wait gave up
-    int pad_;
+    int stream_out;              // ping-pong buffer holding the latest FP32 correction
     unsigned long long maxbits;  // running max |delta| of the current sweep
     double last_max;             // max |delta| of the last full sweep
     double rnorm, bnorm, rmax, rel;
@@ -55,6 +55,7 @@ struct SolverWorkspace {
     size_t cells = 0;           // capacity in elements of the per-cell buffers
     uint8_t *mask = nullptr;    // neighbour-validity bits per cell
     float *e32 = nullptr;       // FP32 correction (mixed precision)
+    float *e32b = nullptr;      // second FP32 correction buffer (ping-pong stream sweeps)
     float *r32 = nullptr;       // FP32 right-hand side of the correction equation
     double *partials = nullptr; // per-block reduction partials
     int max_partials = 0;

@@ -137,9 +137,9 @@ __global__ void __launch_bounds__(kBatchThreads, 1) k_sor_batch(BatchArgs a)
         float *base = I.in_smem ? smem_f
                                 : a.gscratch + (size_t)cluster_id * a.gscratch_per_cluster + (size_t)g * P.cta_stride;
         carve(P, base, nmax);
-        const int KH2 = P.KHp >> 1;
-        const int RP = blockDim.x / KH2;
-        const int k = 2 * (threadIdx.x % KH2), rg = threadIdx.x / KH2;
+        const int KH4 = P.KHp >> 2;
+        const int RP = blockDim.x / KH4;
+        const int k = 4 * (threadIdx.x % KH4), rg = threadIdx.x / KH4;
         const bool active = rg < RP;
 
         zero_own_rows(P, n);
@@ -165,7 +165,7 @@ __global__ void __launch_bounds__(kBatchThreads, 1) k_sor_batch(BatchArgs a)
                 for (int c = 0; c < 2; c++) {
                     fetch_halo_plane(cl, P, c ^ 1, g, C, n, G.H);
                     __syncthreads();
-                    if (active) relax_pair(P, c, n, r0, G, k, rg, RP);
+                    if (active) relax_quad(P, c, n, r0, G, k, rg, RP);
                     cl.sync();
                 }
                 ++cyc;

@@ -68,10 +68,10 @@ __global__ void __launch_bounds__(kClusterThreads, 1) k_sor_cluster(ClusterArgs 
     const double rstart = *(volatile const double *)&ctl->rnorm;
     const double stop_abs = 0.5 * a.tol * bnorm;       // verify in FP64 below this
     const double drop_abs = a.drop * rstart;
-    // thread -> (slot pair, row group)
-    const int KH2 = P.KHp >> 1;
-    const int RP = blockDim.x / KH2;
-    const int k = 2 * (threadIdx.x % KH2), rg = threadIdx.x / KH2;
+    // thread -> (slot quad, row group)
+    const int KH4 = P.KHp >> 2;
+    const int RP = blockDim.x / KH4;
+    const int k = 4 * (threadIdx.x % KH4), rg = threadIdx.x / KH4;
     const bool active = rg < RP;
     cl.sync();
 
@@ -80,7 +80,7 @@ __global__ void __launch_bounds__(kClusterThreads, 1) k_sor_cluster(ClusterArgs 
         for (int c = 0; c < 2; c++) {
             fetch_halo_plane(cl, P, c ^ 1, g, C, n, a.H);
             __syncthreads();
-            if (active) relax_pair(P, c, n, r0, G, k, rg, RP);
+            if (active) relax_quad(P, c, n, r0, G, k, rg, RP);
             cl.sync();
         }
         ++sweeps;

@@ -151,6 +151,65 @@ __device__ __forceinline__ void relax_pair(const Planes &P, int c, int n, int r0
     }
 }
 
+// One half sweep of colour c over the band with four slots per thread: slots
+// k..k+3 (k a multiple of 4) of rows lr = 1 + rg, 1 + rg + RP, ...  Five
+// 16-byte shared loads and one store per four cells; the neighbour one slot
+// beyond the quad (left of its first cell when q = 1, right of its last when
+// q = 0) is the only scalar load.  Reads of slot k-1 at k = 0 and of slot
+// KHp at k = KHp-4 fall in the previous / next row of the plane (rows 0..n+1
+// exist) and are used only for cells without that neighbour.
+__device__ __forceinline__ void relax_quad(const Planes &P, int c, int n, int r0, const Grid &G, int k, int rg, int RP)
+{
+    const int W = G.W, H = G.H, KHp = P.KHp;
+    float *__restrict__ own = P.e(c);
+    const float *__restrict__ oth = P.e(c ^ 1);
+    const float *__restrict__ rhs = P.r(c);
+    const float w4 = G.w4;
+#pragma unroll 1
+    for (int lr = 1 + rg; lr <= n; lr += RP) {
+        const int y = r0 + lr - 1;
+        const int s = (y & 1) ^ c;     // x = 2 * slot + s
+        const int q = 1 - s;           // left neighbour slot = slot - q
+        const size_t ro = (size_t)lr * KHp;
+        float4 v = *reinterpret_cast<float4 *>(own + ro + k);
+        const float4 rh = *reinterpret_cast<const float4 *>(rhs + ro - KHp + k);
+        const float4 up = *reinterpret_cast<const float4 *>(oth + ro - KHp + k);
+        const float4 dn = *reinterpret_cast<const float4 *>(oth + ro + KHp + k);
+        const float4 mid = *reinterpret_cast<const float4 *>(oth + ro + k);
+        const float extra = oth[ro + (q ? k - 1 : k + 4)];
+        // left / right neighbours of the four cells
+        const float l0 = q ? extra : mid.x, r0v = q ? mid.x : mid.y;
+        const float l1 = q ? mid.x : mid.y, r1v = q ? mid.y : mid.z;
+        const float l2 = q ? mid.y : mid.z, r2v = q ? mid.z : mid.w;
+        const float l3 = q ? mid.z : mid.w, r3v = q ? mid.w : extra;
+        const int x0 = 2 * k + s;
+        if (y > 0 && y < H - 1 && x0 > 0 && x0 + 7 < W) {
+            v.x = fmaf(w4, fmaf(-4.f, v.x, (l0 + r0v) + (up.x + dn.x)) - rh.x, v.x);
+            v.y = fmaf(w4, fmaf(-4.f, v.y, (l1 + r1v) + (up.y + dn.y)) - rh.y, v.y);
+            v.z = fmaf(w4, fmaf(-4.f, v.z, (l2 + r2v) + (up.z + dn.z)) - rh.z, v.z);
+            v.w = fmaf(w4, fmaf(-4.f, v.w, (l3 + r3v) + (up.w + dn.w)) - rh.w, v.w);
+        } else {
+            const bool hu = y > 0, hd = y < H - 1;
+            const float ls[4] = {l0, l1, l2, l3}, rs[4] = {r0v, r1v, r2v, r3v};
+            const float us[4] = {up.x, up.y, up.z, up.w}, ds[4] = {dn.x, dn.y, dn.z, dn.w};
+            const float rr[4] = {rh.x, rh.y, rh.z, rh.w};
+            float vv[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                const int x = x0 + 2 * j;
+                if (x >= W) continue;
+                const bool hl = x > 0, hr = x + 1 < W;
+                const float sum = ((hu ? us[j] : 0.f) + (hd ? ds[j] : 0.f)) + ((hl ? ls[j] : 0.f) + (hr ? rs[j] : 0.f));
+                const int cnt = (int)hu + (int)hd + (int)hl + (int)hr;
+                const float w = cnt == 4 ? w4 : cnt == 3 ? G.w3 : cnt == 2 ? G.w2 : cnt == 1 ? G.w1 : G.w0;
+                vv[j] = vv[j] + w * (sum - (float)cnt * vv[j] - rr[j]);
+            }
+            v = make_float4(vv[0], vv[1], vv[2], vv[3]);
+        }
+        *reinterpret_cast<float4 *>(own + ro + k) = v;
+    }
+}
+
 // Sum over own cells of (r32 - L e)^2, both colours; FP32 per thread (a few
 // dozen cells), FP64 across threads -- the FP64 pipe of this part is 1/56 of
 // the FP32 one, so per-cell FP64 arithmetic would dominate the check.

@@ -16,7 +16,7 @@ from conftest import load_golden, solver_case_names
 pytestmark = pytest.mark.gpu
 
 RTOL_PLAIN = 1e-5
-SCHEDS = [1, 2]  # launch-per-half-sweep, persistent (4 = fused stripes, 3 = cluster)
+SCHEDS = [1, 2]  # launch-per-half-sweep, persistent (4 = fused stripes, 3 = cluster, 5 = stream)
 
 
 def _rel_mod_const(x, ref):
@@ -47,7 +47,7 @@ def test_legacy_poisson_solver_matches_reference(name):
     assert e2 < RTOL_PLAIN, (name, e2, emax)
 
 
-@pytest.mark.parametrize("sched", SCHEDS)
+@pytest.mark.parametrize("sched", SCHEDS + [5])
 @pytest.mark.parametrize("prec", [0, 1])
 def test_stats_and_reference_stop_semantics(ctx, sched, prec):
     import poisson_caustic_design_gb300 as pcd
@@ -92,7 +92,50 @@ def test_stripes_on_grid_beyond_chip(ctx, prec):
     phi = np.zeros_like(b)
     st = ctx.solve(b, phi, pcd.SolveOptions(stop=pcd.STOP_REL_RESIDUAL, tol=1e-8, max_iterations=100000,
                                             omega=-1.0, precision=prec))
-    assert st["converged"] and st["schedule_used"] == 4   # 1800/148 rows x 2048 x 16 B exceed shared memory
+    # 1800/148 rows x 2048 x 16 B exceed shared memory: FP64 sweeps run the
+    # in-place stripes, FP32 correction sweeps the ping-pong stream kernel
+    assert st["converged"] and st["schedule_used"] == (5 if prec else 4)
+    assert _rel_mod_const(phi, oracle.dct_solve(b))[0] < 1e-6
+
+
+@pytest.mark.parametrize("n,m,ld", [(2048, 1800, 2048), (4096, 300, 4096), (1000, 37, 1000), (1001, 50, 1004),
+                                    (128, 3, 128), (4093, 40, 4096)])
+def test_stream_sweeps_match_launch_schedule(ctx, n, m, ld):
+    """The ping-pong stream sweeps (one pass per sweep from one FP32 buffer
+    into the other, stripe-edge red rows recomputed) run the same red-black
+    iteration as the launch-per-half-sweep kernels: after the same odd number
+    of mixed-precision sweeps (the last one lands in the second buffer) the
+    iterates agree to FP32 rounding.  Covers one and two 4-cell groups per
+    thread, partial last groups (width not a multiple of 4) and short grids."""
+    import torch
+
+    import poisson_caustic_design_gb300 as pcd
+
+    b = pcd.inputs.poisson_rhs(n, 9, "binary", m=m)
+    bd = torch.zeros((m, ld), dtype=torch.float64, device="cuda")[:, :n]
+    bd.copy_(torch.from_numpy(b))
+    out = {}
+    for sched in (1, 5):
+        pd = torch.zeros((m, ld), dtype=torch.float64, device="cuda")[:, :n]
+        st = ctx.solve_device(bd, pd, pcd.SolveOptions(stop=pcd.STOP_REL_RESIDUAL, tol=0.0, max_iterations=37,
+                                                       precision=pcd.PREC_MIXED, omega=-1.0, schedule=sched))
+        assert st["sweeps"] == 37 and st["schedule_used"] == sched
+        out[sched] = pd.cpu().numpy()
+    assert np.isfinite(out[5]).all()
+    err = np.abs(out[5] - out[1]).max() / np.abs(out[1]).max()
+    assert err < 1e-5, err
+
+
+def test_stream_sweeps_reach_exact_solve(ctx):
+    """Two 4-cell groups per thread (4096 columns) to 1e-8 against the DCT solve."""
+    import oracle
+    import poisson_caustic_design_gb300 as pcd
+
+    b = pcd.inputs.poisson_rhs(4096, 12, "gaussian", m=512)
+    phi = np.zeros_like(b)
+    st = ctx.solve(b, phi, pcd.SolveOptions(stop=pcd.STOP_REL_RESIDUAL, tol=1e-8, max_iterations=200000,
+                                            omega=-1.0, precision=pcd.PREC_MIXED, schedule=5))
+    assert st["converged"] and st["schedule_used"] == 5
     assert _rel_mod_const(phi, oracle.dct_solve(b))[0] < 1e-6
 
 
