@@ -313,6 +313,7 @@ def run_ours(args, rank, world, local, pg):
         e2e_ms.append((time.perf_counter() - t) * 1e3)
     barrier(pg)
     e2e = max_over_ranks(pg, float(np.mean(e2e_ms)))
+    print("e2e samples (ms): " + " ".join(f"{t:.2f}" for t in e2e_ms), file=sys.stderr, flush=True)
 
     # roofline of the dominant kernel: the persistent FP32 sweep kernel.
     # Algorithmic bytes per cell-sweep: 12 (read e, read r32, write e in FP32).

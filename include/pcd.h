@@ -74,6 +74,9 @@ typedef struct {
     int warm_start;          /* pcd_warm_start: 1 phi holds the initial guess (reference
                                 behaviour); 0 start at 0; 2 the learned prediction */
     int schedule;            /* pcd_schedule */
+    double refine_drop;      /* mixed precision, cluster and batch schedules: an FP32 cycle ends
+                                once its residual estimate fell by this factor (then the FP64
+                                residual is refreshed); 0 = auto (3e-2) */
 } pcd_solve_opts;
 
 typedef enum {

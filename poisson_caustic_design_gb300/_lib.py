@@ -56,6 +56,7 @@ class SolveOpts(C.Structure):
         ("refine_every", C.c_int),
         ("warm_start", C.c_int),
         ("schedule", C.c_int),
+        ("refine_drop", C.c_double),
     ]
 
 

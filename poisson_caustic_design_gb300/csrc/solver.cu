@@ -810,7 +810,7 @@ namespace {
 // next cycle is launched before the previous one's control block is read; a
 // cycle launched after convergence returns at once.
 int solve_cluster(SolverWorkspace &ws, const double *b, double *phi, const SolveArgs &a, const pcd_solve_opts &o,
-                  int C, size_t smem, int khp, pcd_solve_stats *stats, cudaStream_t s)
+                  int C, size_t smem, int khp, int depth, pcd_solve_stats *stats, cudaStream_t s)
 {
     const int rblocks = grid_blocks((long)a.W * a.H);
     PCD_CUDA(cudaMemsetAsync(ws.e32, 0, sizeof(float) * (size_t)a.H * a.ld, s));
@@ -827,9 +827,10 @@ int solve_cluster(SolverWorkspace &ws, const double *b, double *phi, const Solve
     ca.cycle_cap = o.refine_every > 0 ? o.refine_every : 2048;
     ca.max_iter = a.max_iter;
     ca.tol = a.tol;
-    ca.drop = 3e-2;
+    ca.drop = o.refine_drop > 0.0 ? o.refine_drop : 3e-2;
     for (int c = 0; c < 5; c++) ca.w32[c] = a.w32[c];
     ca.one_minus_omega = (float)(1.0 - a.omega);
+    ca.depth = depth;
 
     PCD_CUDA(cudaEventRecord(ws.k0, s));
     long launched = 0;
@@ -952,10 +953,10 @@ int solve_device(SolverWorkspace &ws, const double *b, double *phi, int W, int H
 
     if (!done_already && !masked && precision == PCD_PREC_MIXED && a.stop == PCD_STOP_REL_RESIDUAL &&
         (o.schedule == PCD_SCHED_AUTO || o.schedule == PCD_SCHED_CLUSTER)) {
-        int C = 0, khp = 0;
+        int C = 0, khp = 0, depth = 0;
         size_t smem = 0;
-        if (cluster_plan(ws.dev, W, H, &C, &smem, &khp) == PCD_OK)
-            return solve_cluster(ws, b, phi, a, o, C, smem, khp, stats, s);
+        if (cluster_plan(ws.dev, W, H, 2, &C, &smem, &khp, &depth) == PCD_OK)
+            return solve_cluster(ws, b, phi, a, o, C, smem, khp, depth, stats, s);
     }
     if (!done_already && !masked &&
         (o.schedule == PCD_SCHED_AUTO || o.schedule == PCD_SCHED_PERSISTENT || o.schedule == PCD_SCHED_CLUSTER)) {

@@ -82,14 +82,10 @@ __device__ void refine(cg::cluster_group &cl, const Planes &P, const BatchInst &
         s_part2[0] = ar;
         s_part2[1] = ab;
     }
-    cl.sync();
-    double tr = 0.0, tb = 0.0;
-    for (int qq = 0; qq < C; qq++) {
-        const double *pp = cl.map_shared_rank(s_part2, qq);
-        tr += pp[0];
-        tb += pp[1];
-    }
-    cl.sync();  // partials read, and every CTA is done reading its neighbours' phi
+    double tr, tb;
+    // ends with a cluster barrier: partials read, and every CTA is done
+    // reading its neighbours' phi
+    cluster_sum2(cl, s_part2, s_red, C, tr, tb);
     r2 = tr;
     b2 = tb;
     if (!init) {
@@ -140,7 +136,6 @@ __global__ void __launch_bounds__(kBatchThreads, 1) k_sor_batch(BatchArgs a)
         const int KH4 = P.KHp >> 2;
         const int RP = blockDim.x / KH4;
         const int k = 4 * (threadIdx.x % KH4), rg = threadIdx.x / KH4;
-        const bool active = rg < RP;
 
         zero_own_rows(P, n);
         if (!a.warm_start)
@@ -165,7 +160,7 @@ __global__ void __launch_bounds__(kBatchThreads, 1) k_sor_batch(BatchArgs a)
                 for (int c = 0; c < 2; c++) {
                     fetch_halo_plane(cl, P, c ^ 1, g, C, n, G.H);
                     __syncthreads();
-                    if (active) relax_quad(P, c, n, r0, G, k, rg, RP);
+                    relax_quad(P, c, n, r0, G, k, rg, RP);
                     cl.sync();
                 }
                 ++cyc;
@@ -175,13 +170,11 @@ __global__ void __launch_bounds__(kBatchThreads, 1) k_sor_batch(BatchArgs a)
                     fetch_halo_plane(cl, P, 0, g, C, n, G.H);
                     fetch_halo_plane(cl, P, 1, g, C, n, G.H);
                     __syncthreads();
-                    const double v = block_sum(residual_sq(P, n, r0, G), s_red);
+                    const double v = block_sum((double)residual_rows_quad(P.e0, P.e1, P.r0, P.r1, -(long)P.KHp, 1,
+                                                                          n + 1, r0 - 1, G, P.KHp, k, rg, RP),
+                                               s_red);
                     if (threadIdx.x == 0) s_part[0] = v;
-                    cl.sync();
-                    double tot = 0.0;
-                    for (int qq = 0; qq < C; qq++) tot += *cl.map_shared_rank(s_part, qq);
-                    cl.sync();
-                    const double est = sqrt(tot);
+                    const double est = sqrt(cluster_sum(cl, s_part, s_red, C));
                     if (cap || est <= stop_abs || est <= drop_abs) break;
                 }
             }
@@ -338,7 +331,7 @@ int batch_solve_device(BatchWorkspace &ws, int dev, const pcd_instance *inst, in
     ba.gscratch_per_cluster = gper;
     ba.check_every = o.check_every > 0 ? o.check_every : 16;
     ba.cycle_cap = o.refine_every > 0 ? o.refine_every : 4096;
-    ba.drop = 3e-2;
+    ba.drop = o.refine_drop > 0.0 ? o.refine_drop : 3e-2;
     ba.warm_start = o.warm_start ? 1 : 0;
     cfg.gridDim = dim3(ncl * C);
     cfg.stream = s;

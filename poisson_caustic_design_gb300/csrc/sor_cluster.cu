@@ -22,6 +22,7 @@
 // `drop` (the FP32 iteration cannot resolve much more than two digits of the
 // correction) or is below half the stop tolerance, or at the sweep caps; the
 // FP64 residual then decides convergence.
+#include <algorithm>
 #include <cooperative_groups.h>
 
 #include "sor_cluster.cuh"
@@ -72,7 +73,6 @@ __global__ void __launch_bounds__(kClusterThreads, 1) k_sor_cluster(ClusterArgs 
     const int KH4 = P.KHp >> 2;
     const int RP = blockDim.x / KH4;
     const int k = 4 * (threadIdx.x % KH4), rg = threadIdx.x / KH4;
-    const bool active = rg < RP;
     cl.sync();
 
     int sweeps = 0;
@@ -80,7 +80,7 @@ __global__ void __launch_bounds__(kClusterThreads, 1) k_sor_cluster(ClusterArgs 
         for (int c = 0; c < 2; c++) {
             fetch_halo_plane(cl, P, c ^ 1, g, C, n, a.H);
             __syncthreads();
-            if (active) relax_quad(P, c, n, r0, G, k, rg, RP);
+            relax_quad(P, c, n, r0, G, k, rg, RP);
             cl.sync();
         }
         ++sweeps;
@@ -89,7 +89,8 @@ __global__ void __launch_bounds__(kClusterThreads, 1) k_sor_cluster(ClusterArgs 
             fetch_halo_plane(cl, P, 0, g, C, n, a.H);
             fetch_halo_plane(cl, P, 1, g, C, n, a.H);
             __syncthreads();
-            double v = residual_sq(P, n, r0, G);
+            double v = (double)residual_rows_quad(P.e0, P.e1, P.r0, P.r1, -(long)P.KHp, 1, n + 1, r0 - 1, G, P.KHp,
+                                                  k, rg, RP);
             v = warp_sum(v);
             if ((threadIdx.x & 31) == 0) s_red[threadIdx.x >> 5] = v;
             __syncthreads();
@@ -98,12 +99,8 @@ __global__ void __launch_bounds__(kClusterThreads, 1) k_sor_cluster(ClusterArgs 
                 for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += s_red[w];
                 s_part[0] = t;
             }
-            cl.sync();
             // every CTA sums the same partials in the same order
-            double tot = 0.0;
-            for (int qq = 0; qq < C; qq++) tot += *cl.map_shared_rank(s_part, qq);
-            const double est = sqrt(tot);
-            cl.sync();
+            const double est = sqrt(cluster_sum(cl, s_part, s_red, C));
             if (cap || est <= stop_abs || est <= drop_abs) break;
         }
     }
@@ -119,45 +116,317 @@ __global__ void __launch_bounds__(kClusterThreads, 1) k_sor_cluster(ClusterArgs 
     cl.sync();
 }
 
+// ---------------------------------------------------------------------------
+// Temporally blocked variant: K sweeps per halo exchange.  CTA g keeps its n
+// own rows at plane rows [HK, HK + n) and HK = 2K halo rows on each side, of
+// both colours of e and of r32.  Sweep t of a round relaxes red on the rows
+// within d = 2(K - t) - 1 of the band and black within d - 1, recomputing the
+// halo rows the neighbours own; the values are bit-identical to the owners'
+// (same inputs, same arithmetic), so after K sweeps the own rows equal K
+// red-black sweeps of the whole grid.  The own boundary rows are then copied
+// to an export buffer of the round's parity; after one cluster barrier each
+// CTA copies its neighbours' exports into its halo rows.  A CTA rewrites an
+// export buffer only two rounds later, after the barrier that follows its
+// neighbours' reads, so one barrier per round suffices.
+template <int K>
+struct TBPlanes {
+    static constexpr int HK = 2 * K;
+    float *e[2];    // colour planes of e, rows [0, n + 2 HK)
+    float *r[2];    // colour planes of r32, same rows
+    float *ex;      // exports: [parity][side: 0 top, 1 bottom][colour][HK rows][KHp]
+    int KHp;
+    __device__ __forceinline__ float *exp_row(int par, int side, int c, int i) const
+    {
+        return ex + ((size_t)(((par * 2 + side) * 2 + c) * HK + i)) * KHp;
+    }
+};
+
+template <int K>
+__host__ __device__ inline size_t tb_floats(int nmax, int KHp)
+{
+    constexpr int HK = 2 * K;
+    return (size_t)4 * (nmax + 2 * HK) * KHp + (size_t)8 * HK * KHp;
+}
+
+// Colour c on plane rows [lo, hi) intersected with the thread's row block
+// [rb0, rb1), walked top-down: the other colour's rows lr-1, lr, lr+1 stay in
+// registers from one row to the next (one new 16-byte load of them per row).
+// With SHFL (a warp lies within one row group and its lanes hold consecutive
+// quads) the neighbour one slot beyond the quad comes from the adjacent lane;
+// the first / last lane of the warp load it.
+// The first / last quad of an interior row after the interior form: the
+// cell at x = 0 lacks its left neighbour, the one at x = W-1 its right one
+// (three neighbours, both when W = 1), cells past the last column keep v.
+__device__ __forceinline__ float4 quad_edge_fix(float4 nv, const float4 &v, const float4 &rh, const float4 &up,
+                                               const float4 &dn, const float4 &mid, float extra, int q, int x0,
+                                               int W, float w2, float w3)
+{
+    const float ls[4] = {q ? extra : mid.x, q ? mid.x : mid.y, q ? mid.y : mid.z, q ? mid.z : mid.w};
+    const float rs[4] = {q ? mid.x : mid.y, q ? mid.y : mid.z, q ? mid.z : mid.w, q ? mid.w : extra};
+    const float us[4] = {up.x, up.y, up.z, up.w}, ds[4] = {dn.x, dn.y, dn.z, dn.w};
+    const float rr[4] = {rh.x, rh.y, rh.z, rh.w}, vv[4] = {v.x, v.y, v.z, v.w};
+    float out[4] = {nv.x, nv.y, nv.z, nv.w};
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+        const int x = x0 + 2 * j;
+        if (x >= W) {
+            out[j] = vv[j];
+        } else if (x == 0 || x == W - 1) {
+            const bool hl = x > 0, hr = x + 1 < W;
+            const float sum = (us[j] + ds[j]) + ((hl ? ls[j] : 0.f) + (hr ? rs[j] : 0.f));
+            const int cnt = 2 + (int)hl + (int)hr;
+            out[j] = vv[j] + (cnt == 3 ? w3 : w2) * (sum - (float)cnt * vv[j] - rr[j]);
+        }
+    }
+    return make_float4(out[0], out[1], out[2], out[3]);
+}
+
+__device__ __forceinline__ float4 lds4(unsigned a)
+{
+    float4 v;
+    asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];" : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w) : "r"(a));
+    return v;
+}
+__device__ __forceinline__ float lds1(unsigned a)
+{
+    float v;
+    asm volatile("ld.shared.f32 %0, [%1];" : "=f"(v) : "r"(a));
+    return v;
+}
+__device__ __forceinline__ void sts4(unsigned a, const float4 &v)
+{
+    asm volatile("st.shared.v4.f32 [%0], {%1, %2, %3, %4};" ::"r"(a), "f"(v.x), "f"(v.y), "f"(v.z), "f"(v.w)
+                 : "memory");
+}
+
+template <bool SHFL>
+__device__ __forceinline__ void tb_relax_block(float *own_p, const float *oth_p, const float *rhs_p, int c, int lo,
+                                               int hi, int rb0, int rb1, int ybase, const Grid &G, int KHp, int k)
+{
+    const int W = G.W, H = G.H;
+    const float w4 = G.w4, w3 = G.w3, w2 = G.w2;
+    const int l0 = max(lo, rb0), l1 = min(hi, rb1);
+    const int lane = threadIdx.x & 31;
+    // 32-bit shared-memory addresses of slot k of row 0 of each plane
+    const unsigned row_bytes = 4u * (unsigned)KHp;
+    const unsigned own = (unsigned)__cvta_generic_to_shared(own_p) + 4u * k;
+    const unsigned oth = (unsigned)__cvta_generic_to_shared(oth_p) + 4u * k;
+    const unsigned rhs = (unsigned)__cvta_generic_to_shared(rhs_p) + 4u * k;
+    float4 up = make_float4(0.f, 0.f, 0.f, 0.f), mid = up, dn = up;
+    if (l0 < l1) {
+        up = lds4(oth + (unsigned)(l0 - 1) * row_bytes);
+        mid = lds4(oth + (unsigned)l0 * row_bytes);
+    }
+    // parity of the first cell's column: s = (y & 1) ^ c, flips every row
+    int s = ((ybase + l0) & 1) ^ c;
+#pragma unroll 1
+    for (int lr = l0; lr < l1; lr++, s ^= 1) {
+        const unsigned ro = (unsigned)lr * row_bytes;
+        dn = lds4(oth + ro + row_bytes);
+        const int y = ybase + lr;
+        const int q = 1 - s;
+        float extra;
+        if (SHFL) {
+            // one shuffle per row: the direction is uniform across the warp
+            extra = q ? __shfl_up_sync(0xffffffffu, mid.w, 1) : __shfl_down_sync(0xffffffffu, mid.x, 1);
+            if (q ? lane == 0 : lane == 31) extra = lds1(oth + ro + (q ? -4 : 16));
+        } else {
+            extra = lds1(oth + ro + (q ? -4 : 16));
+        }
+        if (y >= 0 && y < H) {
+            const float4 v = lds4(own + ro);
+            const float4 rh = lds4(rhs + ro);
+            const int x0 = 2 * k + s;
+            float4 nv;
+            if (y > 0 && y < H - 1) {
+                nv = quad_interior(v, rh, up, dn, mid, extra, q, w4);
+                if (x0 == 0 || x0 + 7 >= W) nv = quad_edge_fix(nv, v, rh, up, dn, mid, extra, q, x0, W, w2, w3);
+            } else {
+                nv = quad_general(v, rh, up, dn, mid, extra, q, x0, y, W, H, G.w0, G.w1, G.w2, G.w3, w4);
+            }
+            sts4(own + ro, nv);
+        }
+        up = mid;
+        mid = dn;
+    }
+}
+
+template <int K>
+__global__ void __launch_bounds__(kClusterThreads, 1) k_sor_cluster_tb(ClusterArgs a)
+{
+    constexpr int HK = 2 * K;
+    cg::cluster_group cl = cg::this_cluster();
+    extern __shared__ __align__(16) float smem_f[];
+    __shared__ double s_part[1];
+    __shared__ double s_red[32];
+    const int C = (int)cl.num_blocks(), g = (int)cl.block_rank(), W = a.W, H = a.H;
+    int r0, n;
+    band_of(g, C, H, r0, n);
+    const int nmax = (H + C - 1) / C;
+    const int KHp = a.khp;
+    const int rows = nmax + 2 * HK;
+    TBPlanes<K> P;
+    P.KHp = KHp;
+    P.e[0] = smem_f;
+    P.e[1] = smem_f + (size_t)rows * KHp;
+    P.r[0] = smem_f + (size_t)2 * rows * KHp;
+    P.r[1] = smem_f + (size_t)3 * rows * KHp;
+    P.ex = smem_f + (size_t)4 * rows * KHp;
+    Grid G;
+    G.W = W; G.H = H;
+    G.w0 = a.w32[0]; G.w1 = a.w32[1]; G.w2 = a.w32[2]; G.w3 = a.w32[3]; G.w4 = a.w32[4];
+
+    const Ctl *ctl = a.ctl;
+    if (*(volatile const int *)&ctl->done) return;  // speculative launch after convergence: all CTAs agree
+    const int ybase = r0 - HK;  // grid row of plane row 0
+    // own and halo rows of e and r32 from global memory (zero outside the grid)
+    for (int t = threadIdx.x; t < (n + 2 * HK) * KHp * 2; t += blockDim.x) {
+        const int lr = t / (2 * KHp), x = t - lr * 2 * KHp, y = ybase + lr;
+        const int c = (x + y) & 1;
+        float ev = 0.f, rv = 0.f;
+        if (y >= 0 && y < H && x < W) {
+            const size_t gi = (size_t)y * a.ld + x;
+            ev = a.e[gi];
+            rv = a.r32[gi];
+        }
+        (c ? P.e[1] : P.e[0])[(size_t)lr * KHp + (x >> 1)] = ev;
+        (c ? P.r[1] : P.r[0])[(size_t)lr * KHp + (x >> 1)] = rv;
+    }
+    const int done_before = *(volatile const int *)&ctl->sweeps;
+    const double bnorm = *(volatile const double *)&ctl->bnorm;
+    const double rstart = *(volatile const double *)&ctl->rnorm;
+    const double stop_abs = 0.5 * a.tol * bnorm;
+    const double drop_abs = a.drop * rstart;
+    const int KH4 = KHp >> 2;
+    const int RP = blockDim.x / KH4;
+    const int k = 4 * (threadIdx.x % KH4), rg = threadIdx.x / KH4;
+    const int K4 = KHp >> 2;
+    // contiguous row blocks over the relaxed span [1, n + 2 HK - 1); warps
+    // within one row group when a row group is a whole number of warps
+    const int span = n + 2 * HK - 2, L = (span + RP - 1) / RP;
+    const int rb0 = rg < RP ? 1 + rg * L : 0, rb1 = rg < RP ? min(rb0 + L, n + 2 * HK - 1) : 0;
+    const bool shfl = (KH4 & 31) == 0;
+    __syncthreads();
+
+    int sweeps = 0, par = 0, next_check = a.check_every;
+    for (;;) {
+        // kr <= K sweeps on the band and its halo (fewer at the sweep caps)
+        const int kr = min(K, min(a.cycle_cap - sweeps, a.max_iter - done_before - sweeps));
+        for (int t = 0; t < kr; t++) {
+            const int d = 2 * (kr - t) - 1;
+            if (shfl) {
+                tb_relax_block<true>(P.e[0], P.e[1], P.r[0], 0, HK - d, HK + n + d, rb0, rb1, ybase, G, KHp, k);
+                __syncthreads();
+                tb_relax_block<true>(P.e[1], P.e[0], P.r[1], 1, HK - d + 1, HK + n + d - 1, rb0, rb1, ybase, G, KHp, k);
+            } else {
+                tb_relax_block<false>(P.e[0], P.e[1], P.r[0], 0, HK - d, HK + n + d, rb0, rb1, ybase, G, KHp, k);
+                __syncthreads();
+                tb_relax_block<false>(P.e[1], P.e[0], P.r[1], 1, HK - d + 1, HK + n + d - 1, rb0, rb1, ybase, G, KHp,
+                                      k);
+            }
+            __syncthreads();
+        }
+        sweeps += kr;
+        // export the own boundary rows, one barrier, import the neighbours'
+        for (int i = threadIdx.x; i < 2 * 2 * HK * K4; i += blockDim.x) {
+            const int q4 = i % K4, rest = i / K4, row = rest % HK, cs = rest / HK, c = cs & 1, side = cs >> 1;
+            const int lr = side == 0 ? HK + row : n + row;
+            reinterpret_cast<float4 *>(P.exp_row(par, side, c, row))[q4] =
+                reinterpret_cast<const float4 *>((c ? P.e[1] : P.e[0]) + (size_t)lr * KHp)[q4];
+        }
+        cl.sync();
+        for (int i = threadIdx.x; i < 2 * 2 * HK * K4; i += blockDim.x) {
+            const int q4 = i % K4, rest = i / K4, row = rest % HK, cs = rest / HK, c = cs & 1, side = cs >> 1;
+            // side 0: my top halo <- upper neighbour's bottom export; side 1: my bottom halo <- lower neighbour's top
+            const int nb = side == 0 ? g - 1 : g + 1;
+            if (nb < 0 || nb >= C) continue;
+            const float *src = cl.map_shared_rank(P.exp_row(par, side ^ 1, c, row), nb);
+            const int lr = side == 0 ? row : HK + n + row;
+            reinterpret_cast<float4 *>((c ? P.e[1] : P.e[0]) + (size_t)lr * KHp)[q4] =
+                reinterpret_cast<const float4 *>(src)[q4];
+        }
+        par ^= 1;
+        __syncthreads();
+        const bool cap = sweeps >= a.cycle_cap || done_before + sweeps >= a.max_iter;
+        if (sweeps >= next_check || cap) {
+            next_check = sweeps + a.check_every;
+            double v = (double)residual_rows_quad(P.e[0], P.e[1], P.r[0], P.r[1], 0, HK, HK + n, ybase, G, KHp, k,
+                                                  rg, RP);
+            v = warp_sum(v);
+            if ((threadIdx.x & 31) == 0) s_red[threadIdx.x >> 5] = v;
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                double tt = 0.0;
+                for (int w = 0; w < (int)(blockDim.x >> 5); w++) tt += s_red[w];
+                s_part[0] = tt;
+            }
+            const double est = sqrt(cluster_sum(cl, s_part, s_red, C));
+            if (cap || est <= stop_abs || est <= drop_abs) break;
+        }
+    }
+    for (int t = threadIdx.x; t < n * W; t += blockDim.x) {
+        const int row = t / W, x = t - row * W, y = r0 + row;
+        a.e[(size_t)y * a.ld + x] = (((x + y) & 1) ? P.e[1] : P.e[0])[(size_t)(row + HK) * KHp + (x >> 1)];
+    }
+    if (g == 0 && threadIdx.x == 0) {
+        volatile Ctl *cc = a.ctl;
+        cc->sweeps = done_before + sweeps;
+        if (done_before + sweeps >= a.max_iter) cc->halt = 1;
+    }
+    cl.sync();
+}
+
 }  // namespace
 
-int cluster_plan(int dev, int W, int H, int *C_out, size_t *smem_out, int *khp_out)
+int cluster_plan(int dev, int W, int H, int max_depth, int *C_out, size_t *smem_out, int *khp_out, int *depth_out)
 {
     int max_smem = 0, cluster_ok = 0;
     PCD_CUDA(cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
     PCD_CUDA(cudaDeviceGetAttribute(&cluster_ok, cudaDevAttrClusterLaunch, dev));
     if (!cluster_ok) return PCD_BAD_ARG;
+    const int khp = ((W + 1) / 2 + 3) / 4 * 4;
+    if (khp / 2 > kClusterThreads) return PCD_BAD_ARG;
     for (int C : {16, 8}) {
         if (H < 2 * C) continue;
-        const int nmax = (H + C - 1) / C;
-        const int khp = ((W + 1) / 2 + 3) / 4 * 4;
-        if (khp / 2 > kClusterThreads) continue;
-        const size_t smem = (size_t)(2 * (nmax + 2) + 2 * nmax) * khp * sizeof(float);
-        if (smem + 2048 > (size_t)max_smem) continue;
-        PCD_CUDA(cudaFuncSetAttribute((const void *)k_sor_cluster, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
-        PCD_CUDA(cudaFuncSetAttribute((const void *)k_sor_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      (int)smem));
-        cudaLaunchConfig_t cfg = {};
-        cfg.gridDim = dim3(C);
-        cfg.blockDim = dim3(kClusterThreads);
-        cfg.dynamicSmemBytes = smem;
-        cudaLaunchAttribute attr[1];
-        attr[0].id = cudaLaunchAttributeClusterDimension;
-        attr[0].val.clusterDim.x = C;
-        attr[0].val.clusterDim.y = 1;
-        attr[0].val.clusterDim.z = 1;
-        cfg.attrs = attr;
-        cfg.numAttrs = 1;
-        int nclusters = 0;
-        if (cudaOccupancyMaxActiveClusters(&nclusters, (const void *)k_sor_cluster, &cfg) != cudaSuccess) {
-            cudaGetLastError();
-            continue;
+        const int nmax = (H + C - 1) / C, nmin = H / C;
+        // deepest blocking that fits, then the per-half-sweep exchange
+        for (int depth = std::min(max_depth, 2); depth >= 0; depth--) {
+            size_t smem;
+            const void *fn;
+            if (depth == 0) {
+                smem = (size_t)(2 * (nmax + 2) + 2 * nmax) * khp * sizeof(float);
+                fn = (const void *)k_sor_cluster;
+            } else {
+                if (nmin < 2 * depth) continue;
+                smem = (depth == 2 ? tb_floats<2>(nmax, khp) : tb_floats<1>(nmax, khp)) * sizeof(float);
+                fn = depth == 2 ? (const void *)k_sor_cluster_tb<2> : (const void *)k_sor_cluster_tb<1>;
+            }
+            if (smem + 2048 > (size_t)max_smem) continue;
+            PCD_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+            PCD_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            cudaLaunchConfig_t cfg = {};
+            cfg.gridDim = dim3(C);
+            cfg.blockDim = dim3(kClusterThreads);
+            cfg.dynamicSmemBytes = smem;
+            cudaLaunchAttribute attr[1];
+            attr[0].id = cudaLaunchAttributeClusterDimension;
+            attr[0].val.clusterDim.x = C;
+            attr[0].val.clusterDim.y = 1;
+            attr[0].val.clusterDim.z = 1;
+            cfg.attrs = attr;
+            cfg.numAttrs = 1;
+            int nclusters = 0;
+            if (cudaOccupancyMaxActiveClusters(&nclusters, fn, &cfg) != cudaSuccess) {
+                cudaGetLastError();
+                continue;
+            }
+            if (nclusters < 1) continue;
+            *C_out = C;
+            *smem_out = smem;
+            *khp_out = khp;
+            *depth_out = depth;
+            return PCD_OK;
         }
-        if (nclusters < 1) continue;
-        *C_out = C;
-        *smem_out = smem;
-        *khp_out = khp;
-        return PCD_OK;
     }
     return PCD_BAD_ARG;
 }
@@ -176,7 +445,9 @@ int launch_cluster(ClusterArgs &a, int C, size_t smem, cudaStream_t s)
     attr[0].val.clusterDim.z = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    PCD_CUDA(cudaLaunchKernelEx(&cfg, k_sor_cluster, a));
+    if (a.depth == 2) PCD_CUDA(cudaLaunchKernelEx(&cfg, k_sor_cluster_tb<2>, a));
+    else if (a.depth == 1) PCD_CUDA(cudaLaunchKernelEx(&cfg, k_sor_cluster_tb<1>, a));
+    else PCD_CUDA(cudaLaunchKernelEx(&cfg, k_sor_cluster, a));
     count_launches(1);
     return PCD_OK;
 }

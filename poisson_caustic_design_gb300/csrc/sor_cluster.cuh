@@ -20,11 +20,14 @@ struct ClusterArgs {
     double drop;         // end the cycle when the estimate fell by this factor
     float w32[5];        // omega / cnt
     float one_minus_omega;
+    int depth;           // sweeps between halo exchanges (1 or 2; 0: one exchange per half sweep)
 };
 
-// Cluster size (16 or 8 CTAs) and dynamic shared memory for a W x H grid;
-// PCD_BAD_ARG when the grid does not fit in one cluster.
-int cluster_plan(int dev, int W, int H, int *C_out, size_t *smem_out, int *khp_out);
+// Cluster size (16 or 8 CTAs), sweeps per halo exchange and dynamic shared
+// memory for a W x H grid; PCD_BAD_ARG when the grid does not fit in one
+// cluster.  max_depth caps the sweeps per exchange (0: the per-half-sweep
+// exchange).
+int cluster_plan(int dev, int W, int H, int max_depth, int *C_out, size_t *smem_out, int *khp_out, int *depth_out);
 int launch_cluster(ClusterArgs &a, int C, size_t smem, cudaStream_t s);
 
 }  // namespace pcd

@@ -151,89 +151,219 @@ __device__ __forceinline__ void relax_pair(const Planes &P, int c, int n, int r0
     }
 }
 
-// One half sweep of colour c over the band with four slots per thread: slots
-// k..k+3 (k a multiple of 4) of rows lr = 1 + rg, 1 + rg + RP, ...  Five
-// 16-byte shared loads and one store per four cells; the neighbour one slot
-// beyond the quad (left of its first cell when q = 1, right of its last when
-// q = 0) is the only scalar load.  Reads of slot k-1 at k = 0 and of slot
-// KHp at k = KHp-4 fall in the previous / next row of the plane (rows 0..n+1
-// exist) and are used only for cells without that neighbour.
-__device__ __forceinline__ void relax_quad(const Planes &P, int c, int n, int r0, const Grid &G, int k, int rg, int RP)
+// Four cells of colour c at slots k..k+3 of one plane row (x0 = 2k + s is
+// the column of the first).  `extra` is the neighbour one slot beyond the
+// quad: left of its first cell when q = 1, right of its last when q = 0.
+// Interior form: every cell has four neighbours.
+__device__ __forceinline__ float4 quad_interior(float4 v, const float4 &rh, const float4 &up, const float4 &dn,
+                                               const float4 &mid, float extra, int q, float w4)
 {
-    const int W = G.W, H = G.H, KHp = P.KHp;
-    float *__restrict__ own = P.e(c);
-    const float *__restrict__ oth = P.e(c ^ 1);
-    const float *__restrict__ rhs = P.r(c);
+    const float l0 = q ? extra : mid.x, r0v = q ? mid.x : mid.y;
+    const float l1 = q ? mid.x : mid.y, r1v = q ? mid.y : mid.z;
+    const float l2 = q ? mid.y : mid.z, r2v = q ? mid.z : mid.w;
+    const float l3 = q ? mid.z : mid.w, r3v = q ? mid.w : extra;
+    v.x = fmaf(w4, fmaf(-4.f, v.x, (l0 + r0v) + (up.x + dn.x)) - rh.x, v.x);
+    v.y = fmaf(w4, fmaf(-4.f, v.y, (l1 + r1v) + (up.y + dn.y)) - rh.y, v.y);
+    v.z = fmaf(w4, fmaf(-4.f, v.z, (l2 + r2v) + (up.z + dn.z)) - rh.z, v.z);
+    v.w = fmaf(w4, fmaf(-4.f, v.w, (l3 + r3v) + (up.w + dn.w)) - rh.w, v.w);
+    return v;
+}
+
+// General form (cells without some neighbour, cells past the last column
+// left unchanged): v + omega/cnt * (sum over existing neighbours - cnt v - r).
+static __device__ __noinline__ float4 quad_general(float4 v, float4 rh, float4 up, float4 dn, float4 mid, float extra, int q,
+                                            int x0, int y, int W, int H, float w0, float w1, float w2, float w3,
+                                            float w4)
+{
+    const float ls[4] = {q ? extra : mid.x, q ? mid.x : mid.y, q ? mid.y : mid.z, q ? mid.z : mid.w};
+    const float rs[4] = {q ? mid.x : mid.y, q ? mid.y : mid.z, q ? mid.z : mid.w, q ? mid.w : extra};
+    const float us[4] = {up.x, up.y, up.z, up.w}, ds[4] = {dn.x, dn.y, dn.z, dn.w};
+    const float rr[4] = {rh.x, rh.y, rh.z, rh.w};
+    float vv[4] = {v.x, v.y, v.z, v.w};
+    const bool hu = y > 0, hd = y < H - 1;
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+        const int x = x0 + 2 * j;
+        if (x >= W) continue;
+        const bool hl = x > 0, hr = x + 1 < W;
+        const float sum = ((hu ? us[j] : 0.f) + (hd ? ds[j] : 0.f)) + ((hl ? ls[j] : 0.f) + (hr ? rs[j] : 0.f));
+        const int cnt = (int)hu + (int)hd + (int)hl + (int)hr;
+        const float w = cnt == 4 ? w4 : cnt == 3 ? w3 : cnt == 2 ? w2 : cnt == 1 ? w1 : w0;
+        vv[j] = vv[j] + w * (sum - (float)cnt * vv[j] - rr[j]);
+    }
+    return make_float4(vv[0], vv[1], vv[2], vv[3]);
+}
+
+// Four cells of an interior row (up and down neighbours exist) in the first
+// or last quad of the row: a cell at x = 0 has no left neighbour, one at
+// x = W-1 no right neighbour, cells at x >= W stay unchanged.
+__device__ __forceinline__ float4 quad_row_edge(float4 v, const float4 &rh, const float4 &up, const float4 &dn,
+                                               const float4 &mid, float extra, int q, int x0, int W, float w2,
+                                               float w3, float w4)
+{
+    const float ls[4] = {q ? extra : mid.x, q ? mid.x : mid.y, q ? mid.y : mid.z, q ? mid.z : mid.w};
+    const float rs[4] = {q ? mid.x : mid.y, q ? mid.y : mid.z, q ? mid.z : mid.w, q ? mid.w : extra};
+    const float us[4] = {up.x, up.y, up.z, up.w}, ds[4] = {dn.x, dn.y, dn.z, dn.w};
+    const float rr[4] = {rh.x, rh.y, rh.z, rh.w};
+    float vv[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+        const int x = x0 + 2 * j;
+        const bool hl = x > 0, hr = x + 1 < W;
+        const float sum = (us[j] + ds[j]) + ((hl ? ls[j] : 0.f) + (hr ? rs[j] : 0.f));
+        const int cnt = 2 + (int)hl + (int)hr;
+        const float w = cnt == 4 ? w4 : (cnt == 3 ? w3 : w2);
+        const float nv = vv[j] + w * (sum - (float)cnt * vv[j] - rr[j]);
+        vv[j] = x < W ? nv : vv[j];
+    }
+    return make_float4(vv[0], vv[1], vv[2], vv[3]);
+}
+
+// One half sweep of colour c over plane rows [lo, hi) with four slots per
+// thread: slots k..k+3 (k a multiple of 4) of rows lo + rg, lo + rg + RP, ...
+// (grid row y = ybase + lr; rows outside the grid are skipped; threads with
+// rg >= RP idle).  rhs row lr sits at rhs + lr * KHp + roff.  Five 16-byte
+// shared loads and one store per four cells.  In rows other than the grid's
+// first and last only the first quad (x0 = 0) and the last quad (x0 + 7 >= W)
+// have cells without four neighbours: one lane per row and colour takes the
+// short edge form, the first and last grid rows take the general form on
+// all their lanes.  Reads of slot k-1 at k = 0 and of slot KHp at k = KHp-4
+// fall in the previous / next plane row (both exist) and are used only for
+// cells without that neighbour.
+__device__ __forceinline__ void relax_rows_quad(float *__restrict__ own, const float *__restrict__ oth,
+                                                const float *__restrict__ rhs, long roff, int c, int lo, int hi,
+                                                int ybase, const Grid &G, int KHp, int k, int rg, int RP)
+{
+    const int W = G.W, H = G.H;
     const float w4 = G.w4;
+    if (rg >= RP) return;
 #pragma unroll 1
-    for (int lr = 1 + rg; lr <= n; lr += RP) {
-        const int y = r0 + lr - 1;
-        const int s = (y & 1) ^ c;     // x = 2 * slot + s
-        const int q = 1 - s;           // left neighbour slot = slot - q
+    for (int lr = lo + rg; lr < hi; lr += RP) {
+        const int y = ybase + lr;
+        if (y < 0 || y >= H) continue;
+        const int s = (y & 1) ^ c;   // x = 2 * slot + s
+        const int q = 1 - s;         // left neighbour slot = slot - q
+        const int x0 = 2 * k + s;
         const size_t ro = (size_t)lr * KHp;
-        float4 v = *reinterpret_cast<float4 *>(own + ro + k);
-        const float4 rh = *reinterpret_cast<const float4 *>(rhs + ro - KHp + k);
+        const float4 v = *reinterpret_cast<const float4 *>(own + ro + k);
+        const float4 rh = *reinterpret_cast<const float4 *>(rhs + ro + roff + k);
         const float4 up = *reinterpret_cast<const float4 *>(oth + ro - KHp + k);
         const float4 dn = *reinterpret_cast<const float4 *>(oth + ro + KHp + k);
         const float4 mid = *reinterpret_cast<const float4 *>(oth + ro + k);
         const float extra = oth[ro + (q ? k - 1 : k + 4)];
-        // left / right neighbours of the four cells
-        const float l0 = q ? extra : mid.x, r0v = q ? mid.x : mid.y;
-        const float l1 = q ? mid.x : mid.y, r1v = q ? mid.y : mid.z;
-        const float l2 = q ? mid.y : mid.z, r2v = q ? mid.z : mid.w;
-        const float l3 = q ? mid.z : mid.w, r3v = q ? mid.w : extra;
-        const int x0 = 2 * k + s;
-        if (y > 0 && y < H - 1 && x0 > 0 && x0 + 7 < W) {
-            v.x = fmaf(w4, fmaf(-4.f, v.x, (l0 + r0v) + (up.x + dn.x)) - rh.x, v.x);
-            v.y = fmaf(w4, fmaf(-4.f, v.y, (l1 + r1v) + (up.y + dn.y)) - rh.y, v.y);
-            v.z = fmaf(w4, fmaf(-4.f, v.z, (l2 + r2v) + (up.z + dn.z)) - rh.z, v.z);
-            v.w = fmaf(w4, fmaf(-4.f, v.w, (l3 + r3v) + (up.w + dn.w)) - rh.w, v.w);
+        float4 nv;
+        if (y > 0 && y < H - 1) {
+            if (x0 > 0 && x0 + 7 < W) nv = quad_interior(v, rh, up, dn, mid, extra, q, w4);
+            else nv = quad_row_edge(v, rh, up, dn, mid, extra, q, x0, W, G.w2, G.w3, w4);
         } else {
-            const bool hu = y > 0, hd = y < H - 1;
-            const float ls[4] = {l0, l1, l2, l3}, rs[4] = {r0v, r1v, r2v, r3v};
-            const float us[4] = {up.x, up.y, up.z, up.w}, ds[4] = {dn.x, dn.y, dn.z, dn.w};
-            const float rr[4] = {rh.x, rh.y, rh.z, rh.w};
-            float vv[4] = {v.x, v.y, v.z, v.w};
-#pragma unroll
-            for (int j = 0; j < 4; j++) {
-                const int x = x0 + 2 * j;
-                if (x >= W) continue;
-                const bool hl = x > 0, hr = x + 1 < W;
-                const float sum = ((hu ? us[j] : 0.f) + (hd ? ds[j] : 0.f)) + ((hl ? ls[j] : 0.f) + (hr ? rs[j] : 0.f));
-                const int cnt = (int)hu + (int)hd + (int)hl + (int)hr;
-                const float w = cnt == 4 ? w4 : cnt == 3 ? G.w3 : cnt == 2 ? G.w2 : cnt == 1 ? G.w1 : G.w0;
-                vv[j] = vv[j] + w * (sum - (float)cnt * vv[j] - rr[j]);
-            }
-            v = make_float4(vv[0], vv[1], vv[2], vv[3]);
+            nv = quad_general(v, rh, up, dn, mid, extra, q, x0, y, W, H, G.w0, G.w1, G.w2, G.w3, w4);
         }
-        *reinterpret_cast<float4 *>(own + ro + k) = v;
+        *reinterpret_cast<float4 *>(own + ro + k) = nv;
     }
 }
 
-// Sum over own cells of (r32 - L e)^2, both colours; FP32 per thread (a few
-// dozen cells), FP64 across threads -- the FP64 pipe of this part is 1/56 of
-// the FP32 one, so per-cell FP64 arithmetic would dominate the check.
-__device__ __forceinline__ double residual_sq(const Planes &P, int n, int r0, const Grid &G)
+// Sum of squares of r - L e over the four cells of a quad (cells past the
+// last column excluded), branch free.
+__device__ __forceinline__ float quad_residual_sq(const float4 &v, const float4 &rh, const float4 &up,
+                                                  const float4 &dn, const float4 &mid, float extra, int q, int x0,
+                                                  int y, int W, int H)
 {
-    const int W = G.W, H = G.H, KHp = P.KHp;
+    const float ls[4] = {q ? extra : mid.x, q ? mid.x : mid.y, q ? mid.y : mid.z, q ? mid.z : mid.w};
+    const float rs[4] = {q ? mid.x : mid.y, q ? mid.y : mid.z, q ? mid.z : mid.w, q ? mid.w : extra};
+    const float us[4] = {up.x, up.y, up.z, up.w}, ds[4] = {dn.x, dn.y, dn.z, dn.w};
+    const float rr[4] = {rh.x, rh.y, rh.z, rh.w}, vv[4] = {v.x, v.y, v.z, v.w};
+    const bool hu = y > 0, hd = y < H - 1;
     float acc = 0.f;
-    for (int t = threadIdx.x; t < n * W; t += blockDim.x) {
-        const int row = t / W, x = t - row * W, y = r0 + row;
-        const int c = (x + y) & 1, kk = x >> 1;
-        const size_t ro = (size_t)(row + 1) * KHp;
-        const float *oth = P.e(c ^ 1);
-        const int s = (y & 1) ^ c, q = 1 - s;
-        float sum = 0.f;
-        int cnt = 0;
-        if (x > 0) { sum += oth[ro + kk - q]; cnt++; }
-        if (x < W - 1) { sum += oth[ro + kk - q + 1]; cnt++; }
-        if (y > 0) { sum += oth[ro - KHp + kk]; cnt++; }
-        if (y < H - 1) { sum += oth[ro + KHp + kk]; cnt++; }
-        const float e = P.e(c)[ro + kk];
-        const float r = P.r(c)[ro - KHp + kk] - (sum - (float)cnt * e);
-        acc = fmaf(r, r, acc);
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+        const int x = x0 + 2 * j;
+        const bool hl = x > 0, hr = x + 1 < W;
+        const float sum = ((hu ? us[j] : 0.f) + (hd ? ds[j] : 0.f)) + ((hl ? ls[j] : 0.f) + (hr ? rs[j] : 0.f));
+        const int cnt = (int)hu + (int)hd + (int)hl + (int)hr;
+        const float r = rr[j] - (sum - (float)cnt * vv[j]);
+        acc = x < W ? fmaf(r, r, acc) : acc;
     }
-    return (double)acc;
+    return acc;
+}
+
+// Sum over plane rows [lo, hi) (grid row ybase + lr), both colours, of
+// (r - L e)^2 in FP32 per thread; the same quad mapping as relax_rows_quad.
+__device__ __forceinline__ float residual_rows_quad(const float *__restrict__ e0, const float *__restrict__ e1,
+                                                   const float *__restrict__ r0p, const float *__restrict__ r1p,
+                                                   long roff, int lo, int hi, int ybase, const Grid &G, int KHp,
+                                                   int k, int rg, int RP)
+{
+    float acc = 0.f;
+    if (rg >= RP) return acc;
+    for (int lr = lo + rg; lr < hi; lr += RP) {
+        const int y = ybase + lr;
+        if (y < 0 || y >= G.H) continue;
+        const size_t ro = (size_t)lr * KHp;
+#pragma unroll
+        for (int c = 0; c < 2; c++) {
+            const float *own = c ? e1 : e0, *oth = c ? e0 : e1, *rhs = c ? r1p : r0p;
+            const int s = (y & 1) ^ c, q = 1 - s;
+            const float4 v = *reinterpret_cast<const float4 *>(own + ro + k);
+            const float4 rh = *reinterpret_cast<const float4 *>(rhs + ro + roff + k);
+            const float4 up = *reinterpret_cast<const float4 *>(oth + ro - KHp + k);
+            const float4 dn = *reinterpret_cast<const float4 *>(oth + ro + KHp + k);
+            const float4 mid = *reinterpret_cast<const float4 *>(oth + ro + k);
+            const float extra = oth[ro + (q ? k - 1 : k + 4)];
+            acc += quad_residual_sq(v, rh, up, dn, mid, extra, q, 2 * k + s, y, G.W, G.H);
+        }
+    }
+    return acc;
+}
+
+// Cluster-wide sum of one value per CTA (s_part[0], written before the call
+// by each CTA), identical in every CTA: lanes 0..C-1 of warp 0 read the C
+// partials in parallel and reduce them in a fixed order.  Ends with a
+// cluster barrier, after which s_part may be rewritten.
+__device__ __forceinline__ double cluster_sum(cg::cluster_group &cl, double *s_part, double *s_bcast, int C)
+{
+    cl.sync();
+    if (threadIdx.x < 32) {
+        const int lane = threadIdx.x;
+        double x = lane < C ? *cl.map_shared_rank(s_part, lane) : 0.0;
+        x = warp_sum(x);
+        if (lane == 0) *s_bcast = x;
+    }
+    __syncthreads();
+    const double tot = *s_bcast;
+    cl.sync();
+    return tot;
+}
+
+// Two values per CTA (s_part[0..1]) summed over the cluster the same way.
+__device__ __forceinline__ void cluster_sum2(cg::cluster_group &cl, double *s_part, double *s_bcast, int C,
+                                             double &t0, double &t1)
+{
+    cl.sync();
+    if (threadIdx.x < 32) {
+        const int lane = threadIdx.x;
+        double x = 0.0, z = 0.0;
+        if (lane < C) {
+            const double *pp = cl.map_shared_rank(s_part, lane);
+            x = pp[0];
+            z = pp[1];
+        }
+        x = warp_sum(x);
+        z = warp_sum(z);
+        if (lane == 0) {
+            s_bcast[0] = x;
+            s_bcast[1] = z;
+        }
+    }
+    __syncthreads();
+    t0 = s_bcast[0];
+    t1 = s_bcast[1];
+    cl.sync();
+}
+
+// One half sweep of colour c over the band (plane rows 1..n, rhs rows 0..n-1).
+__device__ __forceinline__ void relax_quad(const Planes &P, int c, int n, int r0, const Grid &G, int k, int rg, int RP)
+{
+    relax_rows_quad(P.e(c), P.e(c ^ 1), P.r(c), -(long)P.KHp, c, 1, n + 1, r0 - 1, G, P.KHp, k, rg, RP);
 }
 
 // Block-wide sum into thread 0 (blockDim a multiple of 32).

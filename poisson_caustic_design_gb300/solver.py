@@ -43,6 +43,7 @@ class SolveOptions:
     refine_every: int = 0
     warm_start: int = 1      # 0 zero, 1 phi is the initial guess, 2 learned prediction
     schedule: int = 0
+    refine_drop: float = 0.0
 
     def to_c(self) -> _lib.SolveOpts:
         o = _lib.SolveOpts()
@@ -55,6 +56,7 @@ class SolveOptions:
         o.refine_every = int(self.refine_every)
         o.warm_start = int(self.warm_start)
         o.schedule = int(self.schedule)
+        o.refine_drop = float(self.refine_drop)
         return o
 
 

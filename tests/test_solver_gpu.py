@@ -126,6 +126,28 @@ def test_stream_sweeps_match_launch_schedule(ctx, n, m, ld):
     assert err < 1e-5, err
 
 
+@pytest.mark.parametrize("n,m", [(512, 512), (96, 80), (640, 480), (33, 17), (1024, 300), (1024, 400)])
+def test_cluster_sweeps_match_launch_schedule(ctx, n, m):
+    """The cluster schedule (FP32 sweeps in distributed shared memory, two or
+    one sweeps per halo exchange with the halo rows recomputed, or one
+    exchange per half sweep when the halo does not fit: 1024 x 400) runs the
+    same red-black iteration as the launch-per-half-sweep kernels: after the
+    same odd number of mixed-precision sweeps (a last round of one sweep) the
+    iterates agree to FP32 rounding."""
+    import poisson_caustic_design_gb300 as pcd
+
+    b = pcd.inputs.poisson_rhs(n, 4, "gaussian", m=m)
+    out = {}
+    for sched in (1, 3):
+        phi = np.zeros_like(b)
+        st = ctx.solve(b, phi, pcd.SolveOptions(stop=pcd.STOP_REL_RESIDUAL, tol=1e-14, max_iterations=37,
+                                                precision=pcd.PREC_MIXED, omega=-1.0, schedule=sched))
+        assert st["sweeps"] == 37 and st["schedule_used"] == sched
+        out[sched] = phi
+    err = np.abs(out[3] - out[1]).max() / np.abs(out[1]).max()
+    assert err < 1e-5, err
+
+
 def test_stream_sweeps_reach_exact_solve(ctx):
     """Two 4-cell groups per thread (4096 columns) to 1e-8 against the DCT solve."""
     import oracle
