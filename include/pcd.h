@@ -83,8 +83,9 @@ typedef enum {
     PCD_WARM_ZERO = 0,
     PCD_WARM_GIVEN = 1,
     /* the context's network (pcd_ctx_set_warm_start_net) predicts phi from b;
-     * the prediction is kept only if its residual is below ||b|| (a zero
-     * guess), otherwise the solve starts from zero (stats->warm_used = 3) */
+     * after 8 Gauss-Seidel sweeps the prediction is kept if its residual is
+     * below that of a zero guess after the same sweeps, otherwise the solve
+     * starts from zero (stats->warm_used = 3) */
     PCD_WARM_LEARNED = 2
 } pcd_warm_start;
 
@@ -118,7 +119,14 @@ typedef struct {
     double sweep_ms;         /* device time of the sweep kernel(s) alone (CUDA events) */
     int schedule_used;       /* pcd_schedule that ran */
     int warm_used;           /* 0 zero, 1 given, 2 learned, 3 learned prediction rejected (zero) */
-    double warm_rel_residual;/* ||b - L phi0|| / ||b|| of the learned prediction (warm_start 2) */
+    double warm_rel_residual;/* warm_start 2: ||b - L phi|| / ||b|| of the learned prediction after
+                                8 Gauss-Seidel sweeps (red-black, omega = 1) */
+    int tuned;               /* 1: the context's autotuner chose the knobs below for this shape */
+    int check_every_used;    /* check_every the solve ran with (0 = the schedule's default) */
+    int refine_every_used;   /* refine_every the solve ran with (0 = default) */
+    double refine_drop_used; /* refine_drop the solve ran with (0 = default) */
+    double warm_zero_rel_residual; /* warm_start 2: the same for a zero guess after the same sweeps;
+                                      the prediction is kept when warm_rel_residual is smaller */
 } pcd_solve_stats;
 
 typedef struct pcd_ctx pcd_ctx;
@@ -182,6 +190,9 @@ typedef struct {
     int cluster_size;        /* CTAs per cluster (one per SM) */
     long long smem_bytes;    /* dynamic shared memory per CTA */
     long long cell_sweeps;   /* sum over instances of width*height*sweeps */
+    int check_every;         /* FP32 sweeps between residual estimates used */
+    double refine_drop;      /* cycle drop factor used */
+    int tuned;               /* 1: the context's autotuner chose cluster size, check_every, refine_drop */
 } pcd_batch_stats;
 
 /* Mixed precision (FP32 sweeps, FP64 defect correction) with the relative-
@@ -190,6 +201,20 @@ typedef struct {
  * whole.  stats has `count` entries in the caller's order. */
 int pcd_batch_solve_device(pcd_ctx *ctx, const pcd_instance *inst, int count, const pcd_solve_opts *opts,
                            pcd_instance_stats *stats, pcd_batch_stats *batch_stats, void *stream);
+
+/* ---- autotuner (no counterpart in the reference) ---------------------------
+ * With autotuning on, the first solve of each (width, height, precision, stop)
+ * with schedule PCD_SCHED_AUTO and check_every, refine_every, refine_drop all
+ * 0, and the first batch of each size signature, time a small set of
+ * candidate settings on the caller's own problem (phi is restored between
+ * trials; the result is that of the winner, solved again from the caller's
+ * phi), keep the fastest that converged and reuse it for later calls of that
+ * shape.  Single solves: check_every, refine_drop, refine_every and the
+ * schedule; batches: cluster size (16 or 8 CTAs), check_every, refine_drop.
+ * Off by default; the trial solves are extra work on the first call only. */
+int pcd_ctx_set_autotune(pcd_ctx *ctx, int enable);
+/* entries: shapes tuned so far; trials: trial solves (or batches) run */
+int pcd_ctx_autotune_info(pcd_ctx *ctx, int *entries, long long *trials);
 
 /* ---- learned warm start (no counterpart in the reference) ------------------
  * A 4-level BF16 U-Net (1->32->64->128->256 channels, 3x3 convolutions, FP32

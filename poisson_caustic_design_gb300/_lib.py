@@ -73,6 +73,11 @@ class SolveStats(C.Structure):
         ("schedule_used", C.c_int),
         ("warm_used", C.c_int),
         ("warm_rel_residual", C.c_double),
+        ("tuned", C.c_int),
+        ("check_every_used", C.c_int),
+        ("refine_every_used", C.c_int),
+        ("refine_drop_used", C.c_double),
+        ("warm_zero_rel_residual", C.c_double),
     ]
 
     def as_dict(self):
@@ -104,7 +109,8 @@ class InstanceStats(C.Structure):
 
 class BatchStats(C.Structure):
     _fields_ = [("device_ms", C.c_double), ("clusters", C.c_int), ("cluster_size", C.c_int),
-                ("smem_bytes", C.c_longlong), ("cell_sweeps", C.c_longlong)]
+                ("smem_bytes", C.c_longlong), ("cell_sweeps", C.c_longlong), ("check_every", C.c_int),
+                ("refine_drop", C.c_double), ("tuned", C.c_int)]
 
 
 _vp = C.c_void_p
@@ -126,6 +132,8 @@ SIGNATURES = {
     "pcd_subtract_average_device": (C.c_int, [_vp, _vp, C.c_int, C.c_int, _vp]),
     "pcd_batch_solve_device": (C.c_int, [_vp, C.POINTER(Instance), C.c_int, C.POINTER(SolveOpts),
                                          C.POINTER(InstanceStats), C.POINTER(BatchStats), _vp]),
+    "pcd_ctx_set_autotune": (C.c_int, [_vp, C.c_int]),
+    "pcd_ctx_autotune_info": (C.c_int, [_vp, C.POINTER(C.c_int), C.POINTER(C.c_longlong)]),
     "pcd_gradient_device": (C.c_int, [_vp, _vp, _vp, _vp, C.c_int, C.c_int, _vp]),
     "pcd_divergence_device": (C.c_int, [_vp, _vp, _vp, _vp, C.c_int, C.c_int, _vp]),
     "pcd_subtract_average_noalloc": (C.c_int, [_vp, C.c_int, C.c_int, _vp]),

@@ -15,6 +15,9 @@
 
 namespace pcd {
 
+// Gauss-Seidel sweeps applied to a learned prediction before it is judged.
+constexpr int kLearnedSmooth = 8;
+
 namespace {
 thread_local std::string g_last_error;
 std::atomic<unsigned long long> g_launches{0};
@@ -66,16 +69,28 @@ int solve_with_warm_start(pcd_ctx *ctx, const double *b, double *phi, int W, int
                           pcd_solve_stats *stats, cudaStream_t s)
 {
     int used = o.warm_start == PCD_WARM_GIVEN ? 1 : 0;
-    double rel0 = -1.0;
+    double rel0 = -1.0, relz = -1.0;
+    int pre_sweeps = 0;
     if (o.warm_start == PCD_WARM_LEARNED) {
         if (!ctx->net) {
             set_error("warm_start = PCD_WARM_LEARNED needs a network (pcd_ctx_set_warm_start_net)");
             return PCD_BAD_ARG;
         }
         PCD_TRY(ctx->net->net.warm_start(b, W, H, ld, phi, s));
-        PCD_TRY(residual_rel(ctx->solver, b, phi, W, H, ld, s, &rel0));
-        if (rel0 < 1.0) {
+        // Judge the prediction after kLearnedSmooth Gauss-Seidel sweeps (red-
+        // black, omega = 1) against a zero guess after the same sweeps: the
+        // sweeps remove the cell-scale error that the prediction's
+        // interpolation and BF16 arithmetic leave (it would dominate the raw
+        // residual), and the zero guess's residual also moves under them.
+        // The prediction is kept when its smoothed residual is the smaller.
+        PCD_TRY(ctx->solver.reserve((size_t)H * ld));
+        double *zero_phi = ctx->solver.r64;  // scratch: the solve rewrites it
+        PCD_TRY(zero_grid(zero_phi, W, H, ld, s));
+        PCD_TRY(smooth_residual(ctx->solver, b, zero_phi, W, H, ld, kLearnedSmooth, 1.0, s, &relz));
+        PCD_TRY(smooth_residual(ctx->solver, b, phi, W, H, ld, kLearnedSmooth, 1.0, s, &rel0));
+        if (rel0 < relz) {
             used = 2;
+            pre_sweeps = kLearnedSmooth;
         } else {  // not better than a zero guess (or not finite): start from zero
             PCD_TRY(zero_grid(phi, W, H, ld, s));
             used = 3;
@@ -85,10 +100,12 @@ int solve_with_warm_start(pcd_ctx *ctx, const double *b, double *phi, int W, int
         set_error("pcd solve: unknown warm_start");
         return PCD_BAD_ARG;
     }
-    int st = solve_device(ctx->solver, b, phi, W, H, ld, o, stats, s);
+    int st = solve_autotuned(ctx, b, phi, W, H, ld, o, stats, s);
     if (stats) {
         stats->warm_used = used;
         stats->warm_rel_residual = rel0;
+        stats->warm_zero_rel_residual = relz;
+        stats->sweeps += pre_sweeps;
     }
     return st;
 }
@@ -175,6 +192,7 @@ int pcd_ctx_destroy(pcd_ctx *ctx)
     ctx->solver.release();
     ctx->grid.release();
     ctx->batch.release();
+    ctx->tuner.release();
     if (ctx->d_b) cudaFree(ctx->d_b);
     if (ctx->d_phi) cudaFree(ctx->d_phi);
     if (ctx->join_in) cudaEventDestroy(ctx->join_in);
@@ -277,7 +295,7 @@ int pcd_batch_solve_device(pcd_ctx *ctx, const pcd_instance *inst, int count, co
     }
     StreamJoin j(ctx, stream);
     PCD_TRY(j.begin());
-    const int st = batch_solve_device(ctx->batch, ctx->device, inst, count, o, stats, batch_stats, j.work);
+    const int st = batch_autotuned(ctx, inst, count, o, stats, batch_stats, j.work);
     PCD_TRY(j.end());
     return st;
 }

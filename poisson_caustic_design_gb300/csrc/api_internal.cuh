@@ -1,13 +1,36 @@
 // api_internal.cuh -- the context object behind pcd_ctx* (internal).
 #pragma once
 
+#include <map>
 #include <mutex>
 #include <set>
+#include <vector>
 
 #include "common.cuh"
 #include "grid.cuh"
 #include "solver.cuh"
 #include "sor_batch.cuh"
+
+namespace pcd {
+// Settings the autotuner picked for one solve shape / batch signature.
+struct TunedSolve {
+    int check_every = 0, refine_every = 0, schedule = PCD_SCHED_AUTO;
+    double refine_drop = 0.0;
+};
+struct TunedBatch {
+    int cluster = 16, check_every = 0;
+    double refine_drop = 0.0;
+};
+struct Autotuner {
+    int enabled = 0;
+    long long trials = 0;
+    std::map<std::vector<long long>, TunedSolve> solves;
+    std::map<std::vector<long long>, TunedBatch> batches;
+    double *save = nullptr;  // phi snapshot between trials
+    size_t save_cells = 0;
+    void release();
+};
+}  // namespace pcd
 
 struct pcd_ctx {
     int device = 0;
@@ -28,6 +51,7 @@ struct pcd_ctx {
     pcd_unet *net = nullptr;
     // networks created on this context; their device state is released with it
     std::set<pcd_unet *> nets;
+    pcd::Autotuner tuner;
 };
 
 namespace pcd {
@@ -45,4 +69,9 @@ int ctx_stage(pcd_ctx *ctx, size_t cells);
 int ctx_activate(pcd_ctx *ctx);
 int solve_with_warm_start(pcd_ctx *ctx, const double *b, double *phi, int W, int H, int ld, pcd_solve_opts o,
                           pcd_solve_stats *stats, cudaStream_t s);
+// solve_device through the context's autotuner (autotune.cu)
+int solve_autotuned(pcd_ctx *ctx, const double *b, double *phi, int W, int H, int ld, const pcd_solve_opts &o,
+                    pcd_solve_stats *stats, cudaStream_t s);
+int batch_autotuned(pcd_ctx *ctx, const pcd_instance *inst, int count, const pcd_solve_opts &o,
+                    pcd_instance_stats *stats, pcd_batch_stats *bstats, cudaStream_t s);
 }  // namespace pcd

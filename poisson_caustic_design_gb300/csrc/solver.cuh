@@ -86,6 +86,10 @@ struct SolverWorkspace {
 int residual_rel(SolverWorkspace &ws, const double *b, const double *phi, int W, int H, int ld, cudaStream_t s,
                  double *rel);
 int zero_grid(double *phi, int W, int H, int ld, cudaStream_t s);
+// `sweeps` red-black sweeps with relaxation factor omega (FP64, NaN cells
+// excluded as in the solver) on phi, then ||b - L phi|| / ||b||.
+int smooth_residual(SolverWorkspace &ws, const double *b, double *phi, int W, int H, int ld, int sweeps, double omega,
+                    cudaStream_t s, double *rel);
 
 int solve_device(SolverWorkspace &ws, const double *b, double *phi, int W, int H, int ld,
                  const pcd_solve_opts &o, pcd_solve_stats *stats, cudaStream_t s);

@@ -234,7 +234,7 @@ void BatchWorkspace::release()
 }
 
 int batch_solve_device(BatchWorkspace &ws, int dev, const pcd_instance *inst, int count, const pcd_solve_opts &o,
-                       pcd_instance_stats *stats, pcd_batch_stats *bstats, cudaStream_t s)
+                       pcd_instance_stats *stats, pcd_batch_stats *bstats, cudaStream_t s, int cluster)
 {
     if (!inst || count < 1) {
         set_error("pcd_batch_solve_device: empty batch");
@@ -244,13 +244,17 @@ int batch_solve_device(BatchWorkspace &ws, int dev, const pcd_instance *inst, in
         set_error("pcd_batch_solve_device: the batch solve takes the relative-residual stop with tol > 0");
         return PCD_BAD_ARG;
     }
-    constexpr int C = 16;
+    if (cluster != 0 && cluster != 8 && cluster != 16) {
+        set_error("pcd_batch_solve_device: cluster size must be 8 or 16");
+        return PCD_BAD_ARG;
+    }
+    const int C = cluster ? cluster : 16;
     for (int i = 0; i < count; i++) {
         const pcd_instance &q = inst[i];
         if (!q.b || !q.phi || q.width < 2 || q.height < 2 * C || q.ld < q.width ||
             plane_stride(q.width) / 2 > kBatchThreads) {
             set_error("pcd_batch_solve_device: instance " + std::to_string(i) +
-                      " needs 2 <= width <= 4096, height >= 32, ld >= width and device arrays");
+                      " needs 2 <= width <= 4096, height >= 2 x cluster size, ld >= width and device arrays");
             return PCD_BAD_ARG;
         }
     }
@@ -293,7 +297,7 @@ int batch_solve_device(BatchWorkspace &ws, int dev, const pcd_instance *inst, in
     int ncl = 0;
     PCD_CUDA(cudaOccupancyMaxActiveClusters(&ncl, (const void *)k_sor_batch, &cfg));
     if (ncl < 1) {
-        set_error("pcd_batch_solve_device: no 16-CTA cluster fits on this device");
+        set_error("pcd_batch_solve_device: no " + std::to_string(C) + "-CTA cluster fits on this device");
         return PCD_BAD_ARG;
     }
     ncl = std::min(ncl, count);
@@ -338,7 +342,10 @@ int batch_solve_device(BatchWorkspace &ws, int dev, const pcd_instance *inst, in
 
     // one CUDA graph per batch signature: upload descriptors, reset the work
     // counter, the persistent launch, read the descriptors (statistics) back
-    std::vector<long long> key = {count, ncl, (long long)smem, ba.check_every, ba.cycle_cap, ba.warm_start};
+    long long drop_bits;
+    std::memcpy(&drop_bits, &ba.drop, 8);
+    std::vector<long long> key = {count, C, ncl, (long long)smem, ba.check_every, ba.cycle_cap, ba.warm_start,
+                                  drop_bits};
     for (int j = 0; j < count; j++) {
         const BatchInst &d = ws.h_inst[j];
         long long tb;
@@ -403,6 +410,9 @@ int batch_solve_device(BatchWorkspace &ws, int dev, const pcd_instance *inst, in
         bstats->cluster_size = C;
         bstats->smem_bytes = (long long)smem;
         bstats->cell_sweeps = cell_sweeps;
+        bstats->check_every = ba.check_every;
+        bstats->refine_drop = ba.drop;
+        bstats->tuned = 0;
     }
     return all ? PCD_OK : PCD_NOT_CONVERGED;
 }

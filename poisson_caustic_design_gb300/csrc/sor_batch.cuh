@@ -45,7 +45,8 @@ struct BatchWorkspace {
     void release();
 };
 
+// cluster: CTAs per cluster (16 or 8; 0 = 16)
 int batch_solve_device(BatchWorkspace &ws, int dev, const pcd_instance *inst, int count, const pcd_solve_opts &o,
-                       pcd_instance_stats *stats, pcd_batch_stats *bstats, cudaStream_t s);
+                       pcd_instance_stats *stats, pcd_batch_stats *bstats, cudaStream_t s, int cluster = 0);
 
 }  // namespace pcd

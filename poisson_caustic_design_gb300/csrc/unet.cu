@@ -33,6 +33,9 @@ namespace pcd {
 namespace {
 
 inline int round32(int k) { return (k + 31) / 32 * 32; }
+
+// binomial filter passes on a prediction before it is interpolated to the grid
+constexpr int kPredFilter = 4;
 inline int grid1d(long n) { return (int)std::max<long>(1, std::min<long>(8192, (n + 255) / 256)); }
 
 // b (FP64, W x H, ld) -> x (FP32, S x S): area-average / nearest resample
@@ -77,9 +80,12 @@ __global__ void k_normalize(const float *x, long n, int B, const float *stats, _
     }
 }
 
-// phi0 (FP64, W x H, ld) = scale * bilinear(phi_hat (S x S)), scale = W*H... (see caller)
-__global__ void k_resample_out(const float *ph, int S, double scale, double *phi, int W, int H, int ld)
+// phi0 (FP64, W x H, ld) = wh * std(x) * bilinear(phi_hat (S x S)), std from
+// stats[1] = 1 / std of the network input
+__global__ void k_resample_out(const float *ph, int S, const float *stats, double wh, double *phi, int W, int H,
+                               int ld)
 {
+    const double scale = wh / (double)stats[1];
     const long total = (long)W * H;
     for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x * blockDim.x) {
         const int y = (int)(t / W), x = (int)(t - (long)y * W);
@@ -91,6 +97,21 @@ __global__ void k_resample_out(const float *ph, int S, double scale, double *phi
         const float v = (1 - ty) * ((1 - tx) * ph[y0 * S + x0] + tx * ph[y0 * S + x1]) +
                         ty * ((1 - tx) * ph[y1 * S + x0] + tx * ph[y1 * S + x1]);
         phi[(size_t)y * ld + x] = scale * (double)v;
+    }
+}
+
+// One pass of the 3x3 binomial filter [1 2 1]^T [1 2 1] / 16 on an S x S
+// field (edge cells reuse the nearest cell).
+__global__ void k_binomial(const float *__restrict__ in, float *__restrict__ out, int S)
+{
+    const long total = (long)S * S;
+    for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x * blockDim.x) {
+        const int y = (int)(t / S), x = (int)(t - (long)y * S);
+        const int ym = max(y - 1, 0), yp = min(y + 1, S - 1), xm = max(x - 1, 0), xp = min(x + 1, S - 1);
+        const float r0 = in[ym * S + xm] + 2.f * in[ym * S + x] + in[ym * S + xp];
+        const float r1 = in[y * S + xm] + 2.f * in[y * S + x] + in[y * S + xp];
+        const float r2 = in[yp * S + xm] + 2.f * in[yp * S + x] + in[yp * S + xp];
+        out[t] = (r0 + 2.f * r1 + r2) * (1.f / 16.f);
     }
 }
 
@@ -470,12 +491,17 @@ int UNet::warm_start(const double *b, int W, int H, int ld, double *phi, cudaStr
     PCD_LAUNCHED(1);
     PCD_TRY(load_input(xin_f, 1, s));
     PCD_TRY(forward(1, s));
-    // phi ~ phi_hat * std(b_resampled) * (grid side)^2; std comes from stats[1] = 1/std
-    float st[2];
-    PCD_CUDA(cudaMemcpyAsync(st, stats, sizeof(st), cudaMemcpyDeviceToHost, s));
-    PCD_CUDA(cudaStreamSynchronize(s));
-    const double scale = (1.0 / st[1]) * (double)W * (double)H;
-    k_resample_out<<<grid1d((long)W * H), 256, 0, s>>>(pred, S, scale, phi, W, H, ld);
+    // phi ~ phi_hat * std(b_resampled) * W * H; std from stats[1] = 1/std on the device
+    // kPredFilter binomial passes on the network grid: the prediction's error
+    // is largest at the scale of the network's cells, where the fine-grid
+    // Laplacian amplifies it most; the filter leaves the large scales that
+    // shorten the solve (ping-pong between pred and dpred, ending in pred)
+    static_assert(kPredFilter % 2 == 0, "the filter passes end in pred");
+    for (int k = 0; k < kPredFilter; k++) {
+        k_binomial<<<grid1d((long)S * S), 256, 0, s>>>(k % 2 ? dpred : pred, k % 2 ? pred : dpred, S);
+        PCD_LAUNCHED(1);
+    }
+    k_resample_out<<<grid1d((long)W * H), 256, 0, s>>>(pred, S, stats, (double)W * (double)H, phi, W, H, ld);
     PCD_LAUNCHED(1);
     return PCD_OK;
 }

@@ -124,12 +124,21 @@ class UNet:
         check(self._L.pcd_ctx_set_warm_start_net((ctx or self.ctx).handle, self._h), "pcd_ctx_set_warm_start_net")
 
 
-def make_pairs(ctx: Context, seeds, S: int = 256, tol: float = 1e-7, chunk: int = 256):
+def make_pairs(ctx: Context, seeds, S: int = 256, tol: float = 1e-7, chunk: int = 256, net_res: int | None = None):
     """Right-hand sides b (Gaussian mixtures for even seeds, binary shapes for
-    odd ones) and their potentials solved on the GPU by the batched solver.
-    Returns CUDA float32 tensors x = b and target = phi / (std(b) * S^2)."""
+    odd ones) on S x S grids and their potentials, solved on the GPU by the
+    batched solver.  With net_res < S both are area-averaged to net_res x
+    net_res (the grid the network runs on; the library averages a solve's b
+    the same way before inference).  Returns CUDA float32 tensors x (the
+    averaged b) and target = averaged phi / (std(x) * S^2), the scaling the
+    library inverts with the std of its averaged input and the solve grid's
+    W * H."""
     import torch
+    import torch.nn.functional as F
 
+    R = net_res or S
+    if S % R:
+        raise ValueError("the data grid must be a multiple of the network grid")
     xs, ts = [], []
     opts = SolveOptions(stop=STOP_REL_RESIDUAL, tol=tol, max_iterations=200000, omega=-1.0, warm_start=0)
     seeds = list(seeds)
@@ -140,6 +149,9 @@ def make_pairs(ctx: Context, seeds, S: int = 256, tol: float = 1e-7, chunk: int 
         phis = [torch.zeros_like(b) for b in bs]
         batch_solve(ctx, bs, phis, opts)
         for b, p in zip(bs, phis):
+            if R != S:
+                b = F.avg_pool2d(b[None, None], S // R)[0, 0]
+                p = F.avg_pool2d(p[None, None], S // R)[0, 0]
             sd = b.std()
             xs.append(b.float())
             ts.append((p / (sd * S * S)).float())
@@ -185,5 +197,5 @@ def train(net: UNet, x, t, epochs: int = 4, batch: int = 16, lr: float = 2e-3, w
     return hist
 
 
-def default_weights_path(resolution: int = 256) -> str:
+def default_weights_path(resolution: int = 64) -> str:
     return os.path.join(os.path.dirname(os.path.abspath(__file__)), "weights", f"unet{resolution}.npz")

@@ -95,6 +95,16 @@ class Context:
         except Exception:
             pass
 
+    def set_autotune(self, enable: bool = True) -> None:
+        """Turn the context's autotuner on or off (pcd_ctx_set_autotune)."""
+        check(self._L.pcd_ctx_set_autotune(self._h, 1 if enable else 0), "pcd_ctx_set_autotune")
+
+    def autotune_info(self) -> dict:
+        """Shapes tuned so far and trial solves run (pcd_ctx_autotune_info)."""
+        e, t = C.c_int(0), C.c_longlong(0)
+        check(self._L.pcd_ctx_autotune_info(self._h, C.byref(e), C.byref(t)), "pcd_ctx_autotune_info")
+        return {"entries": e.value, "trials": t.value}
+
     def solve(self, b: np.ndarray, phi: np.ndarray, opts: SolveOptions | None = None, allow_not_converged=True):
         """Solve L phi = b on host arrays, in place on phi.  Returns stats dict."""
         _as_grid(b, "b")

@@ -1,11 +1,16 @@
 """Train the learned warm start and measure what it gains.
 
     python -m poisson_caustic_design_gb300.train_unet --out weights.npz \\
-        [--pairs 20000] [--resolution 256] [--epochs 6] [--batch 16]
+        [--pairs 20000] [--data-resolution 256] [--resolution 64] [--epochs 30] [--batch 32]
 
 Training pairs come from the library's batched GPU solver (FP32 sweeps, FP64
-defect correction, relative residual 1e-7) on seeded densities: Gaussian
-mixtures for even seeds, binary disk/rectangle fields for odd seeds.  Seeds
+defect correction, relative residual 1e-7) on seeded 256^2 densities:
+Gaussian mixtures for even seeds, binary disk/rectangle fields for odd seeds.
+The network runs on the pairs area-averaged to 64^2: there a 4-level U-Net's
+receptive field (about 90 cells) spans the whole grid, which the Poisson
+inverse needs (at 256^2 it spans a third of it); the library averages a
+solve's right-hand side to the network grid and interpolates the prediction
+back.  Seeds
 from 900000 on are held out for the evaluation, which solves each held-out
 density at 256^2 and 512^2 to relative residual 1e-6 from a zero guess and
 from the network's prediction and reports sweeps and wall time.
@@ -51,17 +56,31 @@ def evaluate(ctx, net, sizes=(256, 512), seeds=range(900000, 900008)):
     return rows
 
 
+def summarize(rows):
+    """Mean sweep and time ratios (learned start / zero start) per grid size."""
+    return {
+        "mean_sweep_ratio": {str(n): float(np.mean([r["sweeps_2"] / r["sweeps_0"] for r in rows if r["n"] == n]))
+                             for n in (256, 512)},
+        "mean_time_ratio": {str(n): float(np.mean([r["ms_2"] / r["ms_0"] for r in rows if r["n"] == n]))
+                            for n in (256, 512)},
+        "accepted": int(sum(r["warm_used"] == 2 for r in rows)), "evaluated": len(rows),
+    }
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--out", required=True)
     ap.add_argument("--pairs", type=int, default=20000)
-    ap.add_argument("--resolution", type=int, default=256)
-    ap.add_argument("--epochs", type=int, default=6)
-    ap.add_argument("--batch", type=int, default=16)
+    ap.add_argument("--resolution", type=int, default=64, help="network grid")
+    ap.add_argument("--data-resolution", type=int, default=256, help="grid of the training solves")
+    ap.add_argument("--epochs", type=int, default=30)
+    ap.add_argument("--batch", type=int, default=32)
     ap.add_argument("--lr", type=float, default=2e-3)
     ap.add_argument("--report", default=None)
     ap.add_argument("--time-budget-s", type=float, default=None)
     ap.add_argument("--half", action="store_true", help="store the weights as float16")
+    ap.add_argument("--evaluate-only", default=None, metavar="WEIGHTS",
+                    help="skip training: evaluate these weights on the held-out seeds")
     args = ap.parse_args()
 
     import torch
@@ -70,11 +89,24 @@ def main():
     from poisson_caustic_design_gb300 import learned
 
     ctx = pcd.Context(0)
+    if args.evaluate_only:
+        net = learned.UNet(ctx, resolution=args.resolution, max_batch=1)
+        net.load(args.evaluate_only)
+        rows = evaluate(ctx, net)
+        for r in rows:
+            print(json.dumps(r), flush=True)
+        summ = summarize(rows)
+        print(json.dumps(summ), flush=True)
+        if args.report:
+            with open(args.report, "w") as f:
+                json.dump({"summary": summ, "rows": rows}, f, indent=1)
+        return
     t0 = time.time()
-    x, t = learned.make_pairs(ctx, range(args.pairs), args.resolution, tol=1e-7)
+    x, t = learned.make_pairs(ctx, range(args.pairs), args.data_resolution, tol=1e-7, net_res=args.resolution)
     torch.cuda.synchronize()
     t_data = time.time() - t0
-    print(f"pairs: {x.shape[0]} at {args.resolution}^2 in {t_data:.1f} s", flush=True)
+    print(f"pairs: {x.shape[0]} solved at {args.data_resolution}^2, network grid {args.resolution}^2, "
+          f"in {t_data:.1f} s", flush=True)
     net = learned.UNet(ctx, resolution=args.resolution, max_batch=args.batch, seed=0)
     t0 = time.time()
     hist = learned.train(net, x, t, epochs=args.epochs, batch=args.batch, lr=args.lr, log=lambda m: print(m, flush=True),
@@ -87,13 +119,9 @@ def main():
     for r in rows:
         print(json.dumps(r), flush=True)
     summ = {
-        "pairs": args.pairs, "resolution": args.resolution, "epochs": args.epochs, "batch": args.batch,
-        "data_s": t_data, "train_s": t_train, "loss": hist,
-        "mean_sweep_ratio": {str(n): float(np.mean([r["sweeps_2"] / r["sweeps_0"] for r in rows if r["n"] == n]))
-                             for n in (256, 512)},
-        "mean_time_ratio": {str(n): float(np.mean([r["ms_2"] / r["ms_0"] for r in rows if r["n"] == n]))
-                            for n in (256, 512)},
-        "accepted": int(sum(r["warm_used"] == 2 for r in rows)), "evaluated": len(rows),
+        "pairs": args.pairs, "resolution": args.resolution, "data_resolution": args.data_resolution,
+        "epochs": args.epochs, "batch": args.batch,
+        "data_s": t_data, "train_s": t_train, "loss": hist, **summarize(rows),
     }
     print(json.dumps(summ), flush=True)
     if args.report:
