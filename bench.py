@@ -3,11 +3,14 @@
 Workload (the single-solve configuration): one 512 x 512 Poisson solve of the
 reference's Neumann operator, b = seeded target density - 1 (16-Gaussian
 mixtures and binary disk/rectangle fields alternating, mean removed in FP64),
-from a zero guess to a relative FP64 residual ||b - L phi|| / ||b|| <= 1e-6.
-A step is one such solve of one instance.  The headline form is FP32 sweeps
-with FP64 defect correction; the plain FP64 form is timed beside it.
+to a relative FP64 residual ||b - L phi|| / ||b|| <= 1e-6.  A step is one
+such solve of one instance.  The headline form is the learned warm start
+(the committed 64^2 U-Net weights) + FP32 sweeps with FP64 defect correction;
+the mixed form from a zero guess and the plain FP64 form are timed beside it.
+The context's autotuner picks each form's settings during the warm-up.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--no-cpu-baseline] [--no-batch] [--headline-only] [--no-autotune]
 
 Prints one JSON line.  `value` = wall time per solve (ms, lower is better)
 with b resident in HBM, measured with CUDA events on the launching stream;
@@ -49,6 +52,10 @@ def parse():
     ap.add_argument("--cpu-budget-s", type=float, default=20.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
+    ap.add_argument("--headline-only", action="store_true",
+                    help="time only the headline form (skips the other forms, the accuracy and end-to-end "
+                         "sections, the batch and the 4096^2 sections): for profiling the headline step")
+    ap.add_argument("--no-autotune", action="store_true", help="solve with the schedules' default settings")
     return ap.parse_args()
 
 
@@ -219,7 +226,7 @@ def run_ours(args, rank, world, local, pg):
     ctx = pcd.Context(local)
     # the context's autotuner picks each form's settings during the warm-up
     # (trial solves on the first call of a shape, outside the timed region)
-    ctx.set_autotune(True)
+    ctx.set_autotune(not args.no_autotune)
     L = _lib.load()
     bs_host = instances()
     bs = [torch.from_numpy(b).to(dev) for b in bs_host]
@@ -244,6 +251,8 @@ def run_ours(args, rank, world, local, pg):
         forms = {"learned_mixed": pcd.SolveOptions(stop=pcd.STOP_REL_RESIDUAL, tol=TOL, max_iterations=200000,
                                                    precision=pcd.PREC_MIXED, omega=-1.0, warm_start=2), **forms}
     headline = "learned_mixed" if net is not None else "mixed"
+    if args.headline_only:
+        forms = {headline: forms[headline]}
 
     def timed(opts, k):
         b = bs[k % len(bs)]
@@ -257,14 +266,15 @@ def run_ours(args, rank, world, local, pg):
 
     results = {}
     launches_before = L.pcd_kernel_launches()
+    # clocks sampled across all timed regions (the forms and the end-to-end runs)
     sampler = ClockSampler(local)
+    sampler.start()
     for name, opts in forms.items():
         for w in range(args.warmup):
             timed(opts, w)
         torch.cuda.synchronize()
         barrier(pg)
         if name == headline:
-            sampler.start()
             launches_before = L.pcd_kernel_launches()
         ms, sweeps, sweep_ms, rels, warm = [], [], [], [], []
         for k in range(args.steps):
@@ -278,7 +288,6 @@ def run_ours(args, rank, world, local, pg):
         barrier(pg)
         if name == headline:
             launches = L.pcd_kernel_launches() - launches_before
-            clocks = sampler.stop()
         results[name] = {"ms": max_over_ranks(pg, float(np.sum(ms))) / args.steps, "sweeps": float(np.mean(sweeps)),
                          "sweep_ms": float(np.mean(sweep_ms)), "max_rel_residual": float(np.max(rels)),
                          "schedule": int(st["schedule_used"]),
@@ -287,46 +296,49 @@ def run_ours(args, rank, world, local, pg):
         if name == "learned_mixed":
             results[name]["warm_accepted"] = int(sum(w == 2 for w in warm))
 
-    # accuracy against an FP64 solve to 1e-12 (the plain FP64 solver, itself
-    # checked against the exact DCT solve in the tests) -- outside timing
-    acc = {}
-    b0 = bs[0]
-    ref = torch.zeros_like(phi)
-    ctx.solve_device(b0, ref, pcd.SolveOptions(stop=pcd.STOP_REL_RESIDUAL, tol=1e-12, max_iterations=400000,
-                                               omega=-1.0, warm_start=False), stream=stream.cuda_stream)
-    for name, opts in forms.items():
-        out = torch.zeros_like(phi)
-        ctx.solve_device(b0, out, opts, stream=stream.cuda_stream)
-        torch.cuda.synchronize()
-        d = (out - out.mean()) - (ref - ref.mean())
-        r = ref - ref.mean()
-        acc[name] = {"l2": float(d.norm() / r.norm()), "max": float(d.abs().max() / r.abs().max())}
+    acc, e2e, e2e_ms = {}, None, []
+    if not args.headline_only:
+        # accuracy against an FP64 solve to 1e-12 (the plain FP64 solver, itself
+        # checked against the exact DCT solve in the tests) -- outside timing
+        b0 = bs[0]
+        ref = torch.zeros_like(phi)
+        ctx.solve_device(b0, ref, pcd.SolveOptions(stop=pcd.STOP_REL_RESIDUAL, tol=1e-12, max_iterations=400000,
+                                                   omega=-1.0, warm_start=False), stream=stream.cuda_stream)
+        for name, opts in forms.items():
+            out = torch.zeros_like(phi)
+            ctx.solve_device(b0, out, opts, stream=stream.cuda_stream)
+            torch.cuda.synchronize()
+            d = (out - out.mean()) - (ref - ref.mean())
+            r = ref - ref.mean()
+            acc[name] = {"l2": float(d.norm() / r.norm()), "max": float(d.abs().max() / r.abs().max())}
 
-    # end to end through the host-array C ABI: pinned b in, phi out
-    mixed = forms[headline]
-    hb = [torch.from_numpy(b).pin_memory() for b in bs_host]
-    hphi = torch.zeros((N_GRID, N_GRID), dtype=torch.float64).pin_memory()
-    for w in range(args.warmup):
-        ctx.solve(hb[w % len(hb)].numpy(), hphi.numpy(), mixed)
-    barrier(pg)
-    e2e_ms = []
-    for k in range(args.steps):
-        flush.zero_()
-        torch.cuda.synchronize()
-        t = time.perf_counter()
-        ctx.solve(hb[k % len(hb)].numpy(), hphi.numpy(), mixed)
-        e2e_ms.append((time.perf_counter() - t) * 1e3)
-    barrier(pg)
-    e2e = max_over_ranks(pg, float(np.mean(e2e_ms)))
-    print("e2e samples (ms): " + " ".join(f"{t:.2f}" for t in e2e_ms), file=sys.stderr, flush=True)
+        # end to end through the host-array C ABI: pinned b in, phi out
+        hopts = forms[headline]
+        hb = [torch.from_numpy(b).pin_memory() for b in bs_host]
+        hphi = torch.zeros((N_GRID, N_GRID), dtype=torch.float64).pin_memory()
+        for w in range(args.warmup):
+            ctx.solve(hb[w % len(hb)].numpy(), hphi.numpy(), hopts)
+        barrier(pg)
+        for k in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            t = time.perf_counter()
+            ctx.solve(hb[k % len(hb)].numpy(), hphi.numpy(), hopts)
+            e2e_ms.append((time.perf_counter() - t) * 1e3)
+        barrier(pg)
+        e2e = max_over_ranks(pg, float(np.mean(e2e_ms)))
+    clocks = sampler.stop()
+    if e2e_ms:
+        print("e2e samples (ms): " + " ".join(f"{t:.2f}" for t in e2e_ms), file=sys.stderr, flush=True)
 
-    # roofline of the dominant kernel: the persistent FP32 sweep kernel.
-    # Algorithmic bytes per cell-sweep: 12 (read e, read r32, write e in FP32).
-    m = results["mixed"]
+    # roofline of the dominant kernel of the headline step: the FP32 cluster
+    # sweep kernel (k_sor_cluster_tb).  Algorithmic bytes per cell-sweep: 12
+    # (read e, read r32, write e in FP32), over the sweep kernels' device time
+    # (CUDA events on the context stream around the cycle loop).
     hm = results[headline]
     cells = N_GRID * N_GRID
-    alg_bytes = 12.0 * cells * m["sweeps"]
-    achieved = alg_bytes / (m["sweep_ms"] * 1e-3) / 1e9
+    alg_bytes = 12.0 * cells * hm["sweeps"]
+    achieved = alg_bytes / (hm["sweep_ms"] * 1e-3) / 1e9
     peaks = {}
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -336,13 +348,15 @@ def run_ours(args, rank, world, local, pg):
     peak = peaks.get("hbm_gbs", 6800.0)
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
             "traffic": None, "peak_source": "measured" if "hbm_gbs" in peaks else "fallback",
-            "kernel": "k_sor_cluster (FP32 sweeps)", "alg_bytes_per_solve": alg_bytes,
-            "note": "512^2 working set is shared-memory resident; DRAM traffic per launch is the band load/store"}
+            "kernel": "k_sor_cluster_tb (FP32 sweeps)", "alg_bytes_per_solve": alg_bytes,
+            "note": "the 512^2 working set stays in the cluster's shared memory for a whole FP32 cycle: "
+                    "the kernel is bound by shared-memory issue and cluster barriers, not HBM; DRAM traffic "
+                    "per launch is the band load and store (ncu summary under profiles/)"}
 
     # batched configuration: 64 instances, sizes uniform in {64..1024}^2, one
     # persistent cluster launch (CUDA graph); FP32 sweeps, FP64 residuals
     batched = None
-    if not args.no_batch:
+    if not args.no_batch and not args.headline_only:
         rs = np.random.default_rng(2024)
         sizes = [int(rs.choice([64, 96, 128, 256, 512, 1024])) for _ in range(64)]
         bb = [pcd.inputs.poisson_rhs_torch(n_, [5000 + i])[0].contiguous() for i, n_ in enumerate(sizes)]
@@ -372,7 +386,7 @@ def run_ours(args, rank, world, local, pg):
     # HBM-bound sweep roofline on 4096^2, 256 sweeps per solve: FP32 stream
     # sweeps (12 B algorithmic per cell-sweep), FP64 in-place stripes (24 B)
     stream_roof = None
-    if not args.no_batch:
+    if not args.no_batch and not args.headline_only:
         n4 = 4096
         b4 = pcd.inputs.poisson_rhs_torch(n4, [77])[0].contiguous()
         p4 = torch.zeros_like(b4)
@@ -390,7 +404,7 @@ def run_ours(args, rank, world, local, pg):
         del b4, p4
 
     cpu = None
-    if rank == 0 and not args.no_cpu_baseline:
+    if rank == 0 and not args.no_cpu_baseline and not args.headline_only:
         sys.path.insert(0, os.path.join(ROOT, "oracle"))
         import oracle
 
@@ -413,18 +427,21 @@ def run_ours(args, rank, world, local, pg):
                                "FP32 sweeps + FP64 defect correction)", "grid": N_GRID, "tol": TOL,
                    "omega": "neumann-optimal",
                    "l2": "flushed before every solve (512 MiB write)", "instances": len(SEEDS),
-                   "autotuned": True,
-                   "schedule": {1: "launches", 2: "persistent", 3: "cluster"}.get(m["schedule"], "?")},
-        "forms": {k: {**v, "err_vs_fp64_1e-12": acc[k]} for k, v in results.items()},
-        "speedup_plain_over_mixed": results["plain_fp64"]["ms"] / m["ms"],
-        "speedup_plain_over_headline": results["plain_fp64"]["ms"] / hm["ms"],
+                   "autotuned": not args.no_autotune,
+                   "schedule": {1: "launches", 2: "persistent", 3: "cluster", 4: "stripes",
+                                5: "stream"}.get(hm["schedule"], "?")},
+        "forms": {k: {**v, "err_vs_fp64_1e-12": acc.get(k)} for k, v in results.items()},
+        "speedup_plain_over_mixed": (results["plain_fp64"]["ms"] / results["mixed"]["ms"]
+                                     if "plain_fp64" in results else None),
+        "speedup_plain_over_headline": (results["plain_fp64"]["ms"] / hm["ms"] if "plain_fp64" in results else None),
         "headline_form": headline,
         "batched": batched,
         "roofline_stream_4096": stream_roof,
         "roofline": roof,
         "cpu_baseline": cpu,
-        "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": cells * 8, "d2h_bytes_per_step": cells * 8},
-        "gpu_launches": int(launches) // args.steps * args.steps,
+        "e2e": ({"value": e2e, "unit": UNIT, "h2d_bytes_per_step": cells * 8, "d2h_bytes_per_step": cells * 8}
+                if e2e is not None else None),
+        "gpu_launches": int(launches),
         "gpu_launches_per_step": int(launches) / args.steps,
         "clocks": clocks,
     }
