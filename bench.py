@@ -56,6 +56,11 @@ def parse():
                     help="time only the headline form (skips the other forms, the accuracy and end-to-end "
                          "sections, the batch and the 4096^2 sections): for profiling the headline step")
     ap.add_argument("--no-autotune", action="store_true", help="solve with the schedules' default settings")
+    ap.add_argument("--stream-only", action="store_true",
+                    help="only the 4096^2 sweep-roofline section (for profiling the stream kernel)")
+    ap.add_argument("--config4", action="store_true",
+                    help="instead of the headline: the full caustic pipeline at a 1024^2 mesh on 4096^2 grids "
+                         "(transport and height iterations, plain FP64 and mixed), one JSON line")
     return ap.parse_args()
 
 
@@ -214,6 +219,38 @@ def run_reference(args, rank, world, pg):
     print(json.dumps(line), flush=True)
 
 
+def stream_section(ctx, stream, peak):
+    """HBM-bound sweep roofline on 4096^2, 256 sweeps per solve: FP32 stream
+    sweeps (12 B algorithmic per cell-sweep), FP64 in-place stripes (24 B)."""
+    import torch
+
+    import poisson_caustic_design_gb300 as pcd
+
+    n4 = 4096
+    b4 = pcd.inputs.poisson_rhs_torch(n4, [77])[0].contiguous()
+    p4 = torch.zeros_like(b4)
+    out = {}
+    for prec, bpc, nm, sch in ((pcd.PREC_MIXED, 12, "fp32_sweeps", pcd.SCHED_STREAM),
+                               (pcd.PREC_FP64, 24, "fp64_sweeps", pcd.SCHED_STRIPES)):
+        o4 = pcd.SolveOptions(stop=pcd.STOP_REL_RESIDUAL, tol=0.0, max_iterations=256, omega=-1.0, precision=prec,
+                              warm_start=0, schedule=sch, refine_every=256)
+        ctx.solve_device(b4, p4, o4, stream=stream.cuda_stream)
+        st4 = ctx.solve_device(b4, p4, o4, stream=stream.cuda_stream)
+        per_sweep = st4["sweep_ms"] * 1e-3 / st4["sweeps"]
+        ach = bpc * n4 * n4 / per_sweep / 1e9
+        out[nm] = {"us_per_sweep": per_sweep * 1e6, "achieved_gbs": ach, "frac_hbm": ach / peak,
+                   "schedule": int(st4["schedule_used"])}
+    return out
+
+
+def measured_hbm_peak():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
 # ---------------------------------------------------------------------------
 def run_ours(args, rank, world, local, pg):
     import torch
@@ -228,6 +265,12 @@ def run_ours(args, rank, world, local, pg):
     # (trial solves on the first call of a shape, outside the timed region)
     ctx.set_autotune(not args.no_autotune)
     L = _lib.load()
+    if args.stream_only:
+        peak, src = measured_hbm_peak()
+        print(json.dumps({"roofline_stream_4096": stream_section(ctx, torch.cuda.current_stream(dev), peak),
+                          "peak_gbs": peak, "peak_source": src}), flush=True)
+        ctx.close()
+        return
     bs_host = instances()
     bs = [torch.from_numpy(b).to(dev) for b in bs_host]
     phi = torch.zeros((N_GRID, N_GRID), dtype=torch.float64, device=dev)
@@ -339,15 +382,9 @@ def run_ours(args, rank, world, local, pg):
     cells = N_GRID * N_GRID
     alg_bytes = 12.0 * cells * hm["sweeps"]
     achieved = alg_bytes / (hm["sweep_ms"] * 1e-3) / 1e9
-    peaks = {}
-    try:
-        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
-            peaks = json.load(f)
-    except OSError:
-        pass
-    peak = peaks.get("hbm_gbs", 6800.0)
+    peak, peak_src = measured_hbm_peak()
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-            "traffic": None, "peak_source": "measured" if "hbm_gbs" in peaks else "fallback",
+            "traffic": None, "peak_source": peak_src,
             "kernel": "k_sor_cluster_tb (FP32 sweeps)", "alg_bytes_per_solve": alg_bytes,
             "note": "the 512^2 working set stays in the cluster's shared memory for a whole FP32 cycle: "
                     "the kernel is bound by shared-memory issue and cluster barriers, not HBM; DRAM traffic "
@@ -383,25 +420,9 @@ def run_ours(args, rank, world, local, pg):
                    "check_every": bst["check_every"], "refine_drop": bst["refine_drop"], "autotuned": bool(bst["tuned"])}
         del bb, pp
 
-    # HBM-bound sweep roofline on 4096^2, 256 sweeps per solve: FP32 stream
-    # sweeps (12 B algorithmic per cell-sweep), FP64 in-place stripes (24 B)
     stream_roof = None
     if not args.no_batch and not args.headline_only:
-        n4 = 4096
-        b4 = pcd.inputs.poisson_rhs_torch(n4, [77])[0].contiguous()
-        p4 = torch.zeros_like(b4)
-        stream_roof = {}
-        for prec, bpc, nm, sch in ((pcd.PREC_MIXED, 12, "fp32_sweeps", pcd.SCHED_STREAM),
-                                   (pcd.PREC_FP64, 24, "fp64_sweeps", pcd.SCHED_STRIPES)):
-            o4 = pcd.SolveOptions(stop=pcd.STOP_REL_RESIDUAL, tol=0.0, max_iterations=256, omega=-1.0, precision=prec,
-                                  warm_start=0, schedule=sch, refine_every=256)
-            ctx.solve_device(b4, p4, o4, stream=stream.cuda_stream)
-            st4 = ctx.solve_device(b4, p4, o4, stream=stream.cuda_stream)
-            per_sweep = st4["sweep_ms"] * 1e-3 / st4["sweeps"]
-            ach = bpc * n4 * n4 / per_sweep / 1e9
-            stream_roof[nm] = {"us_per_sweep": per_sweep * 1e6, "achieved_gbs": ach, "frac_hbm": ach / peak,
-                               "schedule": int(st4["schedule_used"])}
-        del b4, p4
+        stream_roof = stream_section(ctx, stream, peak)
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline and not args.headline_only:
@@ -450,11 +471,84 @@ def run_ours(args, rank, world, local, pg):
     ctx.close()
 
 
+def run_config4(args, local):
+    """Full pipeline at mesh 1024^2 / grid 4096^2 on one target: target-area
+    initialisation, two transport iterations and one height iteration, with the
+    reference's stop rule (max |delta| < 1e-7 transport, 1e-8 height; the
+    Neumann-optimal omega) in plain FP64 and in mixed precision.  The CPU
+    figure is the reference's tile-threaded SOR per-sweep time at 4096^2 on
+    the host cores times the GPU plain form's sweep count (extrapolated: a
+    full CPU iteration takes hours)."""
+    import torch
+
+    import poisson_caustic_design_gb300 as pcd
+
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    ctx = pcd.Context(local)
+    R, N = 1024, 4096
+    img = pcd.inputs.pipeline_image(R, seed=4)
+    out = {"mesh": R, "grid": N, "width": 0.5, "focal_l": 1.5, "thickness": 0.1, "forms": {}}
+    for name, prec in (("plain_fp64", pcd.PREC_FP64), ("mixed", pcd.PREC_MIXED)):
+        tr = pcd.SolveOptions(tol=1e-7, precision=prec, omega=-1.0, max_iterations=200000)
+        hs = pcd.SolveOptions(tol=1e-8, precision=prec, omega=-1.0, max_iterations=200000)
+        d = pcd.CausticDesign(ctx, transport=tr, height_solve=hs)
+        d.set_mesh_resolution(R, R)
+        d.set_domain_resolution(N, N)
+        d.set_mesh_size(0.5, 0.5)
+        d.set_lens_focal_length(1.5)
+        d.set_lens_thickness(0.1)
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        d.initialize_solvers(img)
+        torch.cuda.synchronize()
+        rec = {"init_ms": (time.perf_counter() - t) * 1e3, "transport": []}
+        for it in range(2):
+            t = time.perf_counter()
+            step = d.perform_transport_iteration()
+            torch.cuda.synchronize()
+            st = d.last_solve_stats
+            rec["transport"].append({"ms": (time.perf_counter() - t) * 1e3, "step": step, "sweeps": st["sweeps"],
+                                     "solve_ms": st["device_ms"], "schedule": st["schedule_used"]})
+        t = time.perf_counter()
+        upd = d.perform_height_map_iteration(0)
+        torch.cuda.synchronize()
+        st = d.last_solve_stats
+        rec["height"] = {"ms": (time.perf_counter() - t) * 1e3, "update": upd, "sweeps": st["sweeps"],
+                         "solve_ms": st["device_ms"]}
+        out["forms"][name] = rec
+        d.close()
+    # CPU: per-sweep time of the reference's threaded schedule at 4096^2
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+
+    oracle.build(ref=False)
+    port = oracle.Port()
+    threads = os.cpu_count() or 1
+    b = pcd.inputs.poisson_rhs(N, 3, "gaussian")
+    phi = np.zeros_like(b)
+    port.poisson_solver_threads(b, phi, 2, 0.0, threads)
+    t = time.perf_counter()
+    port.poisson_solver_threads(b, phi, 6, 0.0, threads)
+    per_sweep = (time.perf_counter() - t) / 6
+    plain = out["forms"]["plain_fp64"]
+    cpu_ms = [per_sweep * x["sweeps"] * 1e3 for x in plain["transport"]]
+    seg = int(np.floor(np.sqrt(threads)))
+    out["cpu_reference"] = {"per_sweep_ms": per_sweep * 1e3, "threads": seg * seg,
+                            "transport_ms_extrapolated": cpu_ms,
+                            "note": "per-sweep time x the GPU plain form's sweep count"}
+    print(json.dumps({"config4": out}), flush=True)
+    ctx.close()
+
+
 def main():
     args = parse()
     rank, world, local, pg = dist_setup(args.gpus)
     if args.impl == "reference":
         run_reference(args, rank, world, pg)
+    elif args.config4:
+        if rank == 0:
+            run_config4(args, local)
     else:
         run_ours(args, rank, world, local, pg)
     if pg is not None:

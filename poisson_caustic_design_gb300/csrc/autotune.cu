@@ -65,7 +65,7 @@ std::vector<TunedSolve> solve_candidates(const pcd_solve_opts &o)
         add(32, 0.0, 0, PCD_SCHED_PERSISTENT);
         for (int re : {128, 512}) add(0, 0.0, re, PCD_SCHED_STREAM);
     } else if (o.precision == PCD_PREC_MIXED) {
-        for (int re : {16, 32, 64}) add(0, 0.0, re, PCD_SCHED_AUTO);
+        for (int re : {32, 64, 128}) add(0, 0.0, re, PCD_SCHED_AUTO);
     } else {
         for (int ce : {8, 32}) add(ce, 0.0, 0, PCD_SCHED_AUTO);
         add(32, 0.0, 0, PCD_SCHED_STRIPES);

@@ -464,9 +464,13 @@ int stream_plan(int dev, int W, int H, int ld, bool allow_tma, StreamPlan *p)
     const size_t smem = tma_smem_bytes(wpad);
     const bool tma = allow_tma && smem <= (size_t)max_smem;
     if (tma) {
-        const void *fn = G == 1 ? (const void *)k_sweep_tma<1> : (const void *)k_sweep_tma<2>;
-        PCD_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        PCD_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, fn, T, smem));
+        const void *fns[2] = {G == 1 ? (const void *)k_sweep_tma<1, false> : (const void *)k_sweep_tma<2, false>,
+                              G == 1 ? (const void *)k_sweep_tma<1, true> : (const void *)k_sweep_tma<2, true>};
+        for (const void *fn : fns) PCD_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        int bps_t = 0;
+        PCD_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, fns[0], T, smem));
+        PCD_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps_t, fns[1], T, smem));
+        bps = std::min(bps, bps_t);
     } else if (G == 1) {
         PCD_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_sweep_stream<1, false>, T, 0));
     } else {
@@ -492,11 +496,11 @@ template <bool TRACK>
 void launch_stream_t(const StreamPlan &p, const float *ein, float *eout, const float *r, Ctl *ctl, const SolveArgs &a,
                      int out_idx, cudaStream_t s)
 {
-    if (p.tma && !TRACK) {
+    if (p.tma) {
         if (p.G == 1)
-            k_sweep_tma<1><<<p.ns, p.T, p.smem, s>>>(ein, eout, r, ctl, a, p.R, out_idx, p.wpad, kTmaSpinLimit);
+            k_sweep_tma<1, TRACK><<<p.ns, p.T, p.smem, s>>>(ein, eout, r, ctl, a, p.R, out_idx, p.wpad, kTmaSpinLimit);
         else
-            k_sweep_tma<2><<<p.ns, p.T, p.smem, s>>>(ein, eout, r, ctl, a, p.R, out_idx, p.wpad, kTmaSpinLimit);
+            k_sweep_tma<2, TRACK><<<p.ns, p.T, p.smem, s>>>(ein, eout, r, ctl, a, p.R, out_idx, p.wpad, kTmaSpinLimit);
     } else if (p.G == 1) {
         k_sweep_stream<1, TRACK><<<p.ns, p.T, 0, s>>>(ein, eout, r, ctl, a, p.R, out_idx);
     } else {
@@ -1020,7 +1024,7 @@ int solve_device(SolverWorkspace &ws, const double *b, double *phi, int W, int H
     if (!masked && precision == PCD_PREC_MIXED &&
         (o.schedule == PCD_SCHED_AUTO || o.schedule == PCD_SCHED_STREAM || o.schedule == PCD_SCHED_PERSISTENT ||
          o.schedule == PCD_SCHED_CLUSTER) &&
-        stream_plan(ws.dev, W, H, ld, a.stop == PCD_STOP_REL_RESIDUAL, &sp) == PCD_OK)
+        stream_plan(ws.dev, W, H, ld, true, &sp) == PCD_OK)
         sched = PCD_SCHED_STREAM;
     else if (!masked && H >= 3 && W <= 2 * kRowCellsMax * kStripeThreads && o.schedule != PCD_SCHED_LAUNCHES)
         sched = PCD_SCHED_STRIPES;
@@ -1033,7 +1037,11 @@ int solve_device(SolverWorkspace &ws, const double *b, double *phi, int W, int H
     }
     int chunk;
     if (a.stop == PCD_STOP_MAX_UPDATE)
-        chunk = precision == PCD_PREC_MIXED ? (o.refine_every > 0 ? o.refine_every : 32) : 32;
+        // mixed: FP32 sweeps between FP64 refreshes (the stop test runs after
+        // every sweep either way)
+        chunk = precision == PCD_PREC_MIXED
+                    ? (o.refine_every > 0 ? o.refine_every : std::max(32, std::min(128, std::max(W, H) / 32)))
+                    : 32;
     else if (precision == PCD_PREC_MIXED)
         // the FP64 refresh costs several FP32 sweeps; FP32 can carry ~2 digits
         // of the correction, i.e. hundreds of sweeps on large grids

@@ -330,7 +330,7 @@ __device__ __forceinline__ bool mbar_wait(unsigned long long *bar, unsigned pari
 // window W4[(j + c) & 3] holds e rows y-2+c (c = 0..3) and rr[j & 1] / rr[(j+1)
 // & 1] the r rows y-1 / y.  With P a template argument every slot, register
 // and mbarrier parity below is a compile-time constant up to the bit i & 1.
-template <int G, int P>
+template <int G, bool TRACK, int P>
 __device__ __forceinline__ bool tma_step(float4 (&W4)[4][G], float4 (&rr)[2][G], float *es, float *rs,
                                          unsigned long long *ebar, unsigned long long *rbar,
                                          const float *__restrict__ ein, float *__restrict__ eout,
@@ -388,7 +388,7 @@ __device__ __forceinline__ bool tma_step(float4 (&W4)[4][G], float4 (&rr)[2][G],
         float *sl = es + (size_t)sC * wpad;
         const float lft = lft_ok ? sl[col0 - 1] : 0.f;
         const float rgt = rgt_ok ? sl[col0 + 4 * G] : 0.f;
-        relax_row_groups<G, false>(W4[cC], W4[cB], W4[cD], rC, lft, rgt, col0, y, W, H, par, w, m);
+        relax_row_groups<G, TRACK>(W4[cC], W4[cB], W4[cD], rC, lft, rgt, col0, y, W, H, par, w, m);
 #pragma unroll
         for (int k = 0; k < G; k++) {
             const int col = col0 + 4 * k;
@@ -401,7 +401,7 @@ __device__ __forceinline__ bool tma_step(float4 (&W4)[4][G], float4 (&rr)[2][G],
         const float *sl = es + (size_t)sB * wpad;
         const float lft = lft_ok ? sl[col0 - 1] : 0.f;
         const float rgt = rgt_ok ? sl[col0 + 4 * G] : 0.f;
-        relax_row_groups<G, false>(W4[cB], W4[cA], W4[cC], rB, lft, rgt, col0, yb, W, H, par, w, m);
+        relax_row_groups<G, TRACK>(W4[cB], W4[cA], W4[cC], rB, lft, rgt, col0, yb, W, H, par, w, m);
 #pragma unroll
         for (int k = 0; k < G; k++) {
             const int col = col0 + 4 * k;
@@ -414,7 +414,7 @@ __device__ __forceinline__ bool tma_step(float4 (&W4)[4][G], float4 (&rr)[2][G],
     return false;
 }
 
-template <int G>
+template <int G, bool TRACK>
 __global__ void __launch_bounds__(kStreamThreadsMax, 1)
     k_sweep_tma(const float *__restrict__ ein, float *__restrict__ eout, const float *__restrict__ rhs, Ctl *ctl,
                 SolveArgs a, int R, int out_idx, int wpad, long spin_limit)
@@ -481,14 +481,19 @@ __global__ void __launch_bounds__(kStreamThreadsMax, 1)
     }
     for (int i = 0;; i++) {
 #define PCD_TMA_STEP(PP)                                                                                           \
-    if (tma_step<G, PP>(W4, rr, es, rs, ebar, rbar, ein, eout, rhs, i, ys, y0, y1, W, H, ld, wpad, bytes, e_last,  \
-                        r_last, col0, lft_ok, rgt_ok, w, spin_limit, ok, m))                                       \
+    if (tma_step<G, TRACK, PP>(W4, rr, es, rs, ebar, rbar, ein, eout, rhs, i, ys, y0, y1, W, H, ld, wpad, bytes,   \
+                               e_last, r_last, col0, lft_ok, rgt_ok, w, spin_limit, ok, m))                    \
         break;
         PCD_TMA_STEP(0) PCD_TMA_STEP(1) PCD_TMA_STEP(2) PCD_TMA_STEP(3)
         PCD_TMA_STEP(4) PCD_TMA_STEP(5) PCD_TMA_STEP(6) PCD_TMA_STEP(7)
 #undef PCD_TMA_STEP
     }
     if (!ok) atomicExch(&ctl->error, (int)PCD_TIMEOUT);
+    if (TRACK) {
+        double v[1] = {(double)m};
+        block_reduce<1, 1u>(v);
+        if (threadIdx.x == 0 && v[0] > 0.0) atomicMax(&ctl->maxbits, (unsigned long long)__double_as_longlong(v[0]));
+    }
     __syncthreads();
     if (threadIdx.x == 0) {
         __threadfence();
