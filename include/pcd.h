@@ -202,6 +202,22 @@ typedef struct {
 int pcd_batch_solve_device(pcd_ctx *ctx, const pcd_instance *inst, int count, const pcd_solve_opts *opts,
                            pcd_instance_stats *stats, pcd_batch_stats *batch_stats, void *stream);
 
+/* ---- output files (caustic_design.cpp:55-61, mesh.cpp:608-610,411-414,
+ * utils.cpp:198-307, main.cpp:111-135) ------------------------------------
+ * Host functions: the reference's text, byte for byte, from host arrays
+ * (points: mesh_res_x * mesh_res_y x 3, row-major like Mesh::target_points).
+ * No device work; PCD_BAD_ARG if the file cannot be written. */
+int pcd_write_solid_obj(const double *front_points, const double *back_points, int mesh_res_x, int mesh_res_y,
+                        double thickness, double width, double height, const char *filename);  /* save_solid_obj */
+int pcd_write_grid_svg(const double *points, int mesh_res_x, int mesh_res_y, double width, double height,
+                       const char *filename, double stroke_width);                             /* export_grid_to_svg */
+int pcd_write_heightmap_json(const double *h, int width, int height, const char *filename);   /* save_heightmap_as_json */
+/* From a design's device state: which = 0 save_solid_obj_source, 1 _target. */
+int pcd_design_save_solid_obj(pcd_design *d, int which, const char *filename);
+int pcd_design_export_parameterization_svg(pcd_design *d, const char *filename, double stroke_width);
+int pcd_design_export_inverted_transport_map_svg(pcd_design *d, const char *filename, double stroke_width);
+int pcd_design_save_heightmap_json(pcd_design *d, const char *filename);
+
 /* ---- autotuner (no counterpart in the reference) ---------------------------
  * With autotuning on, the first solve of each (width, height, precision, stop)
  * with schedule PCD_SCHED_AUTO and check_every, refine_every, refine_drop all
@@ -274,7 +290,9 @@ typedef enum {
 typedef enum {
     PCD_VERT_TARGET_POINTS = 10, PCD_VERT_SOURCE_POINTS = 11, PCD_VERT_TARGET_AREAS = 12,
     PCD_VERT_ERRORS = 13, PCD_VERT_NORMALS_X = 14, PCD_VERT_NORMALS_Y = 15,
-    PCD_VERT_GRADIENT_X = 16, PCD_VERT_GRADIENT_Y = 17
+    PCD_VERT_GRADIENT_X = 16, PCD_VERT_GRADIENT_Y = 17,
+    PCD_VERT_INVERTED_MAP = 18   /* n x 3: the inverted transport map of the current target mesh
+                                    (mesh.cpp:348-409), computed on request; z = 0 */
 } pcd_vertex_field;
 
 typedef struct {

@@ -145,6 +145,26 @@ class Caustic_design {
         refresh();
     }
 
+    // output files (caustic_design.cpp:20-26,55-61)
+    void save_solid_obj_target(const std::string &filename)
+    {
+        pcd_legacy::check(pcd_design_save_solid_obj(d_, 1, filename.c_str()), "save_solid_obj_target");
+    }
+    void save_solid_obj_source(const std::string &filename)
+    {
+        pcd_legacy::check(pcd_design_save_solid_obj(d_, 0, filename.c_str()), "save_solid_obj_source");
+    }
+    void export_paramererization_to_svg(const std::string &filename, double line_width)
+    {
+        pcd_legacy::check(pcd_design_export_parameterization_svg(d_, filename.c_str(), line_width),
+                          "export_paramererization_to_svg");
+    }
+    void export_inverted_transport_map(std::string filename, double stroke_width)
+    {
+        pcd_legacy::check(pcd_design_export_inverted_transport_map_svg(d_, filename.c_str(), stroke_width),
+                          "export_inverted_transport_map");
+    }
+
    private:
     pcd_ctx *ctx_ = nullptr;
     pcd_design *d_ = nullptr;
@@ -186,5 +206,16 @@ class Caustic_design {
         mesh->source_points = points(PCD_VERT_SOURCE_POINTS);
     }
 };
+
+// main.cpp:111-135
+inline void save_heightmap_as_json(const std::vector<std::vector<double>> &heightmap, const std::string &filename)
+{
+    const int h = (int)heightmap.size(), w = h ? (int)heightmap[0].size() : 0;
+    std::vector<double> flat((size_t)w * h);
+    for (int y = 0; y < h; y++)
+        for (int x = 0; x < w; x++) flat[(size_t)y * w + x] = heightmap[y][x];
+    if (pcd_write_heightmap_json(flat.data(), w, h, filename.c_str()) != PCD_OK)
+        throw std::runtime_error("Failed to open output file.");
+}
 
 #endif  // PCD_LEGACY_HPP

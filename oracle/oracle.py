@@ -280,10 +280,22 @@ class Ref:
         L.ref_design_get.argtypes = [C.c_void_p, C.c_int, _dp]
         L.ref_design_get.restype = C.c_int
         L.ref_design_destroy.argtypes = [C.c_void_p]
+        L.ref_save_solid_obj.argtypes = [_dp, _dp, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, C.c_char_p]
+        L.ref_export_grid_svg.argtypes = [_dp, C.c_int, C.c_int, C.c_double, C.c_double, C.c_char_p, C.c_double]
 
     @staticmethod
     def available() -> bool:
         return os.path.exists(REF_SO) or os.path.isdir(os.path.join(REF_TREE, "src"))
+
+    def save_solid_obj(self, front, back, nx, ny, thickness, width, height, filename):
+        """save_solid_obj (utils.cpp:198-260) on the structured mesh's triangles."""
+        self.L.ref_save_solid_obj(_f64(front), _f64(back), int(nx), int(ny), float(thickness), float(width),
+                                  float(height), filename.encode())
+
+    def export_grid_svg(self, pts, nx, ny, width, height, filename, stroke_width):
+        """export_grid_to_svg (utils.cpp:262-307)."""
+        self.L.ref_export_grid_svg(_f64(pts), int(nx), int(ny), float(width), float(height), filename.encode(),
+                                   float(stroke_width))
 
     def poisson_solver(self, D, phi, max_iterations=100000, tol=1e-7, threads=1):
         h, w = D.shape
@@ -379,3 +391,15 @@ def rel_err_mod_const(x: np.ndarray, ref: np.ndarray):
     d = x - ref
     nr = np.linalg.norm(ref)
     return float(np.linalg.norm(d) / nr), float(np.abs(d).max() / np.abs(ref).max())
+
+
+def heightmap_json_text(h) -> str:
+    """save_heightmap_as_json, main.cpp:111-135 (main.cpp does not compile
+    here: no png.h).  operator<< on a double with the stream's default
+    precision prints like printf "%g" -- the same formatting the reference's
+    compiled save_solid_obj uses for its vertices, which pins it."""
+    h = np.asarray(h, dtype=np.float64)
+    rows = []
+    for i in range(h.shape[0]):
+        rows.append("  [" + ", ".join("%g" % v for v in h[i]) + "]")
+    return "[\n" + ",\n".join(rows) + ("\n" if rows else "") + "]\n"

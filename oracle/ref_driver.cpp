@@ -127,6 +127,36 @@ int ref_design_get(void *h, int which, double *out)
     return -1;
 }
 
+// save_solid_obj, utils.cpp:198-260, on the structured mesh's triangles
+// (generate_structured_mesh, mesh.cpp:45-64: two per quad, {i, i+1, i+nx} and
+// {i+nx, i+1, i+nx+1}); front / back are nx*ny x 3 points.
+void ref_save_solid_obj(const double *front, const double *back, int nx, int ny, double thickness, double width,
+                        double height, const char *filename)
+{
+    std::vector<std::vector<double>> F, B;
+    for (int i = 0; i < nx * ny; i++) {
+        F.push_back({front[3 * i], front[3 * i + 1], front[3 * i + 2]});
+        B.push_back({back[3 * i], back[3 * i + 1], back[3 * i + 2]});
+    }
+    std::vector<std::vector<int>> tri;
+    for (int y = 0; y < ny - 1; y++)
+        for (int x = 0; x < nx - 1; x++) {
+            const int i = y * nx + x;
+            tri.push_back({i, i + 1, i + nx});
+            tri.push_back({i + nx, i + 1, i + nx + 1});
+        }
+    save_solid_obj(F, B, tri, thickness, width, height, nx, ny, std::string(filename));
+}
+
+// export_grid_to_svg, utils.cpp:262-307; points are nx*ny x 3.
+void ref_export_grid_svg(const double *pts, int nx, int ny, double width, double height, const char *filename,
+                         double stroke_width)
+{
+    std::vector<std::vector<double>> P;
+    for (int i = 0; i < nx * ny; i++) P.push_back({pts[3 * i], pts[3 * i + 1], pts[3 * i + 2]});
+    export_grid_to_svg(P, width, height, nx, ny, std::string(filename), stroke_width);
+}
+
 void ref_design_destroy(void *h)
 {
     auto *d = static_cast<Caustic_design *>(h);

@@ -133,6 +133,13 @@ SIGNATURES = {
     "pcd_batch_solve_device": (C.c_int, [_vp, C.POINTER(Instance), C.c_int, C.POINTER(SolveOpts),
                                          C.POINTER(InstanceStats), C.POINTER(BatchStats), _vp]),
     "pcd_ctx_set_autotune": (C.c_int, [_vp, C.c_int]),
+    "pcd_write_solid_obj": (C.c_int, [_dp, _dp, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, C.c_char_p]),
+    "pcd_write_grid_svg": (C.c_int, [_dp, C.c_int, C.c_int, C.c_double, C.c_double, C.c_char_p, C.c_double]),
+    "pcd_write_heightmap_json": (C.c_int, [_dp, C.c_int, C.c_int, C.c_char_p]),
+    "pcd_design_save_solid_obj": (C.c_int, [_vp, C.c_int, C.c_char_p]),
+    "pcd_design_export_parameterization_svg": (C.c_int, [_vp, C.c_char_p, C.c_double]),
+    "pcd_design_export_inverted_transport_map_svg": (C.c_int, [_vp, C.c_char_p, C.c_double]),
+    "pcd_design_save_heightmap_json": (C.c_int, [_vp, C.c_char_p]),
     "pcd_ctx_autotune_info": (C.c_int, [_vp, C.POINTER(C.c_int), C.POINTER(C.c_longlong)]),
     "pcd_gradient_device": (C.c_int, [_vp, _vp, _vp, _vp, C.c_int, C.c_int, _vp]),
     "pcd_divergence_device": (C.c_int, [_vp, _vp, _vp, _vp, C.c_int, C.c_int, _vp]),

@@ -31,7 +31,7 @@ from .solver import Context, SolveOptions
 
 GRID = {"phi": 0, "h": 1, "raster": 2, "divergence": 3, "norm_x": 4, "norm_y": 5}
 VERT = {"target_points": 10, "source_points": 11, "target_areas": 12, "errors": 13, "normals_x": 14,
-        "normals_y": 15, "vertex_gradient_x": 16, "vertex_gradient_y": 17}
+        "normals_y": 15, "vertex_gradient_x": 16, "vertex_gradient_y": 17, "inverted_map": 18}
 
 
 class CausticDesign:
@@ -104,6 +104,21 @@ class CausticDesign:
         self.last_solve_stats = st.as_dict()
         return upd.value
 
+    # ---- output files (caustic_design.cpp:20-26,55-61) ----
+    def save_solid_obj_target(self, filename: str):
+        check(self._L.pcd_design_save_solid_obj(self._h, 1, filename.encode()), "save_solid_obj_target")
+
+    def save_solid_obj_source(self, filename: str):
+        check(self._L.pcd_design_save_solid_obj(self._h, 0, filename.encode()), "save_solid_obj_source")
+
+    def export_paramererization_to_svg(self, filename: str, line_width: float):
+        check(self._L.pcd_design_export_parameterization_svg(self._h, filename.encode(), float(line_width)),
+              "export_paramererization_to_svg")
+
+    def export_inverted_transport_map(self, filename: str, stroke_width: float):
+        check(self._L.pcd_design_export_inverted_transport_map_svg(self._h, filename.encode(), float(stroke_width)),
+              "export_inverted_transport_map")
+
     # ---- public members (caustic_design.h:16-30, mesh.h:51-52) ----
     def _grid(self, name):
         out = np.empty((self.resolution_y, self.resolution_x))
@@ -151,3 +166,41 @@ class CausticDesign:
                 self._ctx.close()
         except Exception:
             pass
+
+
+# ---- writers from host arrays (utils.cpp:198-307, main.cpp:111-135) ----
+def _pts(a, n):
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    if a.shape != (n, 3):
+        raise ValueError(f"points must be {n} x 3")
+    return a
+
+
+def save_solid_obj(front_points, back_points, res_x: int, res_y: int, thickness: float, width: float, height: float,
+                   filename: str) -> None:
+    """save_solid_obj (utils.cpp:198-260) on the structured mesh's triangles."""
+    n = int(res_x) * int(res_y)
+    f, b = _pts(front_points, n), _pts(back_points, n)
+    L = _lib.load()
+    check(L.pcd_write_solid_obj(f.ctypes.data_as(C.POINTER(C.c_double)), b.ctypes.data_as(C.POINTER(C.c_double)),
+                                int(res_x), int(res_y), float(thickness), float(width), float(height),
+                                filename.encode()), "pcd_write_solid_obj")
+
+
+def export_grid_to_svg(points, width: float, height: float, res_x: int, res_y: int, filename: str,
+                       stroke_width: float) -> None:
+    """export_grid_to_svg (utils.cpp:262-307)."""
+    p = _pts(points, int(res_x) * int(res_y))
+    L = _lib.load()
+    check(L.pcd_write_grid_svg(p.ctypes.data_as(C.POINTER(C.c_double)), int(res_x), int(res_y), float(width),
+                               float(height), filename.encode(), float(stroke_width)), "pcd_write_grid_svg")
+
+
+def save_heightmap_as_json(heightmap, filename: str) -> None:
+    """save_heightmap_as_json (main.cpp:111-135)."""
+    h = np.ascontiguousarray(heightmap, dtype=np.float64)
+    if h.ndim != 2:
+        raise ValueError("heightmap must be 2-D")
+    L = _lib.load()
+    check(L.pcd_write_heightmap_json(h.ctypes.data_as(C.POINTER(C.c_double)), h.shape[1], h.shape[0],
+                                     filename.encode()), "pcd_write_heightmap_json")

@@ -823,6 +823,28 @@ int Design::get_vertices(int which, double *out)
         PCD_CUDA(cudaMemcpyAsync(out, pts_out, sizeof(double) * 3 * nv, cudaMemcpyDeviceToHost, s));
         PCD_CUDA(cudaStreamSynchronize(s));
         return PCD_OK;
+    case PCD_VERT_INVERTED_MAP: {
+        if (!initialized) {
+            set_error("pcd_design_get_vertices: initialize first");
+            return PCD_BAD_ARG;
+        }
+        PCD_TRY(locate(tp, 1, nx, ny, s));
+        QueryGrid g{1, nx, ny, nx, ny, p.width, p.height};
+        unsigned int *miss = (unsigned int *)small;
+        PCD_CUDA(cudaMemsetAsync(miss, 0, sizeof(unsigned int), s));
+        k_inverse_gather<<<nblocks(nv), kT, 0, s>>>(tp, g, owner, inv, miss);
+        PCD_LAUNCHED(1);
+        k_points_out<<<nblocks(nv), kT, 0, s>>>(inv, sz, nx, ny, p.width, p.height, false, pts_out);
+        PCD_LAUNCHED(1);
+        PCD_CUDA(cudaMemcpyAsync(small_host, miss, sizeof(unsigned int), cudaMemcpyDeviceToHost, s));
+        PCD_CUDA(cudaMemcpyAsync(out, pts_out, sizeof(double) * 3 * nv, cudaMemcpyDeviceToHost, s));
+        PCD_CUDA(cudaStreamSynchronize(s));
+        if (*(unsigned int *)small_host) {
+            set_error("inverse map miss: a source vertex lies in no deformed triangle");
+            return PCD_RASTER_MISS;
+        }
+        return PCD_OK;
+    }
     case PCD_VERT_TARGET_AREAS: src = target_areas; break;
     case PCD_VERT_ERRORS: src = errors; break;
     case PCD_VERT_NORMALS_X: src = nrm_x; break;

@@ -10,6 +10,10 @@ Fixtures (all float64, seeded inputs, the reference run with max_threads=1):
   zero and warm starts, ragged sizes, a NaN hole, an iteration cap.
 * utils_cases.npz   -- calculate_gradient / calculate_divergence /
   subtractAverage / scale_matrix_proportional / bilinearInterpolation.
+* writer_cases.npz -- save_solid_obj (utils.cpp:198-260) and
+  export_grid_to_svg (utils.cpp:262-307) output files (bytes) of the
+  reference on seeded point sets: ragged and square meshes, negative heights,
+  %g exponents, the non-square SVG whose second loop uses res_x as bound.
 * pipeline_r{16,32,64}.npz -- Caustic_design replay of main.cpp:216-262 at
   mesh resolution r (grid 4r): per-iteration step sizes, target areas, the
   first iteration's errors/raster, final phi / target points, and after the
@@ -112,11 +116,46 @@ def pipeline(R: O.Ref, res: int, seed: int, width=0.5, focal=1.5, thickness=0.1,
     return len(steps)
 
 
+def writer_cases(R: O.Ref):
+    import tempfile
+
+    rng = np.random.default_rng(77)
+    cases = {}
+
+    def pts(nx, ny, w, h, zlo, zhi, jitter=True):
+        y, x = np.meshgrid(np.arange(ny) * h / (ny - 1), np.arange(nx) * w / (nx - 1), indexing="ij")
+        p = np.stack([x.ravel(), y.ravel(), rng.uniform(zlo, zhi, nx * ny)], axis=1)
+        if jitter:
+            p[:, :2] += rng.normal(0, 0.01 * w, (nx * ny, 2))
+        return p
+
+    with tempfile.TemporaryDirectory() as td:
+        fn = os.path.join(td, "out")
+        obj = [("obj_a", 7, 5, 0.5, 0.35, 0.1, pts(7, 5, 0.5, 0.35, -0.03, 0.02), pts(7, 5, 0.5, 0.35, 0, 0, False)),
+               ("obj_b", 4, 4, 1.0, 1.0, 0.2, pts(4, 4, 1.0, 1.0, 0.0, 0.0), pts(4, 4, 1.0, 1.0, 0.0, 0.02, False)),
+               ("obj_c", 3, 6, 12345.678, 0.001, 1e-7,
+                pts(3, 6, 12345.678, 0.001, -1e-5, 3e4), pts(3, 6, 12345.678, 0.001, -2.0, 2.0))]
+        for name, nx, ny, w, h, th, front, back in obj:
+            R.save_solid_obj(front, back, nx, ny, th, w, h, fn)
+            cases[f"{name}/front"], cases[f"{name}/back"] = front, back
+            cases[f"{name}/params"] = np.array([nx, ny, w, h, th])
+            cases[f"{name}/text"] = np.frombuffer(open(fn, "rb").read(), dtype=np.uint8)
+        svg = [("svg_a", 7, 5, 0.5, 0.35, 0.5), ("svg_b", 5, 7, 0.35, 0.5, 1.0), ("svg_c", 6, 6, 0.5, 0.5, 1.0)]
+        for name, nx, ny, w, h, sw in svg:
+            p = pts(nx, ny, w, h, 0.0, 0.0)
+            R.export_grid_svg(p, nx, ny, w, h, fn, sw)
+            cases[f"{name}/points"] = p
+            cases[f"{name}/params"] = np.array([nx, ny, w, h, sw])
+            cases[f"{name}/text"] = np.frombuffer(open(fn, "rb").read(), dtype=np.uint8)
+    np.savez_compressed(os.path.join(OUT, "writer_cases.npz"), **cases)
+
+
 def main():
     O.build(ref=True)
     R = O.Ref()
     solver_cases(R)
     utils_cases(R)
+    writer_cases(R)
     for res, seed in ((16, 3), (32, 11), (64, 29)):
         n = pipeline(R, res, seed)
         print(f"pipeline r{res}: {n} transport iterations")

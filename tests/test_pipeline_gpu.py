@@ -113,3 +113,44 @@ def test_raster_matches_port_on_deformed_mesh(ctx, port):
     ras_cpu = port.subtract_average(ras_cpu)
     assert np.abs(d.raster - ras_cpu).max() < 1e-12 * np.abs(ras_cpu).max()
     d.close()
+
+
+def test_design_output_files(ctx, port, tmp_path):
+    """The design's file writers (save_solid_obj_source / _target,
+    export_paramererization_to_svg, export_inverted_transport_map and the
+    heightmap JSON) write what the host writers write from the design's public
+    members; the inverted transport map they export equals the C port's on
+    the same target mesh."""
+    import poisson_caustic_design_gb300 as pcd
+
+    z = load_golden("pipeline_r16.npz")
+    d, conv = _design(ctx, z)
+    for _ in range(3):
+        d.perform_transport_iteration()
+    d.perform_height_map_iteration(0)
+    r = d.mesh_res_x
+    tp, sp = d.target_points(), d.source_points()
+
+    def same(write_design, write_host):
+        a, b = tmp_path / "a", tmp_path / "b"
+        write_design(str(a))
+        write_host(str(b))
+        assert a.read_bytes() == b.read_bytes()
+        return a.read_bytes()
+
+    same(d.save_solid_obj_source, lambda f: pcd.save_solid_obj(sp, sp, r, r, d.thickness, d.width, d.height, f))
+    same(d.save_solid_obj_target, lambda f: pcd.save_solid_obj(tp, sp, r, r, d.thickness, d.width, d.height, f))
+    same(lambda f: d.export_paramererization_to_svg(f, 0.5),
+         lambda f: pcd.export_grid_to_svg(tp, d.width, d.height, r, r, f, 0.5))
+    inv = d._vert("inverted_map")
+    same(lambda f: d.export_inverted_transport_map(f, 1.0),
+         lambda f: pcd.export_grid_to_svg(inv, d.width, d.height, r, r, f, 1.0))
+    a = tmp_path / "hj"
+    pcd._lib.check(d._L.pcd_design_save_heightmap_json(d._h, str(a).encode()), "json")
+    b = tmp_path / "hj2"
+    pcd.save_heightmap_as_json(d.h, str(b))
+    assert a.read_bytes() == b.read_bytes()
+    ref_inv, miss = port.inverted_map(tp, sp, r, r, d.width, d.height)
+    assert miss == 0
+    np.testing.assert_allclose(inv[:, :2], ref_inv, rtol=0, atol=1e-12)
+    d.close()
