@@ -43,7 +43,9 @@ typedef enum {
     PCD_TIMEOUT = 4,         /* a bounded device-side wait gave up */
     PCD_RASTER_MISS = 5,     /* a grid sample fell in no triangle (the reference calls exit(0)) */
     PCD_NO_DEVICE = 6,
-    PCD_FALLBACK_USED = 7    /* learned warm start rejected; solved from a zero guess */
+    PCD_FALLBACK_USED = 7,   /* learned warm start rejected; solved from a zero guess */
+    PCD_MESH_SMOOTHED = 8    /* transport iteration: a raster miss was handled by Laplacian smoothing
+                                of the target mesh (raster_miss_policy 1); step is NaN */
 } pcd_status;
 
 typedef enum {
@@ -202,6 +204,31 @@ typedef struct {
 int pcd_batch_solve_device(pcd_ctx *ctx, const pcd_instance *inst, int count, const pcd_solve_opts *opts,
                            pcd_instance_stats *stats, pcd_batch_stats *batch_stats, void *stream);
 
+/* ---- image ingest (main.cpp:13-109) ----------------------------------------
+ * image_to_grid: decode a PNG file (any colour type and bit depth, Adam7)
+ * with the reference's libpng transforms (16-bit -> high byte, palette ->
+ * RGB, gray < 8 bit -> 8 bit, tRNS -> alpha) and convert each pixel to
+ * 0.299 r + 0.587 g + 0.114 b on samples / 255 (main.cpp:91-99); gray images
+ * take r = g = b (the reference mis-reads their 2-byte rows as 4-byte).  Host
+ * code.  gray NULL: only width / height.  gray: height x width doubles. */
+int pcd_image_to_grid(const char *filename, int *width, int *height, double *gray);
+/* The decoder alone: rgba NULL queries the size; else width*height*4 bytes. */
+int pcd_png_decode(const unsigned char *data, size_t size, int *width, int *height, unsigned char *rgba);
+/* resize_image (main.cpp:13-27): host arrays (through the process-wide
+ * context of device 0, like pcd_poisson_solver) or device grids. */
+int pcd_resize_image(const double *in, int old_width, int old_height, double *out, int new_width, int new_height);
+int pcd_resize_image_device(pcd_ctx *ctx, const double *in, int old_width, int old_height, int in_ld, double *out,
+                            int new_width, int new_height, int out_ld, void *stream);
+
+/* Fold handling (no counterpart: the reference exits on a raster miss).
+ * Mesh::laplacian_smoothing (mesh.cpp:534-606) of the target mesh on the
+ * device; the number of triangles of the structured mesh whose signed area
+ * is not positive; replacing the target points (n x 3 host array, z ignored),
+ * e.g. to resume from a saved mesh. */
+int pcd_design_smooth_target_mesh(pcd_design *d, double smoothing_factor);
+int pcd_design_count_folds(pcd_design *d, long long *folds);
+int pcd_design_set_target_points(pcd_design *d, const double *points);
+
 /* ---- output files (caustic_design.cpp:55-61, mesh.cpp:608-610,411-414,
  * utils.cpp:198-307, main.cpp:111-135) ------------------------------------
  * Host functions: the reference's text, byte for byte, from host arrays
@@ -303,6 +330,10 @@ typedef struct {
     double thickness;            /* set_lens_thickness */
     pcd_solve_opts transport;    /* solve options of the transport iterations */
     pcd_solve_opts height_solve; /* solve options of the height iterations */
+    int raster_miss_policy;      /* 0: a raster miss returns PCD_RASTER_MISS (the reference exits,
+                                    mesh.cpp:277-279); 1: smooth the target mesh (factor 0.1, the
+                                    reference's unreached caustic_design.cpp:214-217) and return
+                                    PCD_MESH_SMOOTHED */
 } pcd_design_params;
 
 /* Defaults: the reference's solves (max |delta| < 1e-7 transport,

@@ -207,6 +207,30 @@ class Caustic_design {
     }
 };
 
+// main.cpp:29-109 (the PNG loader; see pcd_image_to_grid)
+inline void image_to_grid(const std::string &filename, std::vector<std::vector<double>> &image_grid)
+{
+    int w = 0, h = 0;
+    if (pcd_image_to_grid(filename.c_str(), &w, &h, nullptr) != PCD_OK)
+        throw std::runtime_error("Failed to open PNG file.");
+    std::vector<double> flat((size_t)w * h);
+    if (pcd_image_to_grid(filename.c_str(), &w, &h, flat.data()) != PCD_OK)
+        throw std::runtime_error("Error during PNG read.");
+    image_grid = pcd_legacy::to_rows(flat, w, h);
+}
+
+// main.cpp:13-27
+inline void resize_image(const std::vector<std::vector<double>> &input_image,
+                         std::vector<std::vector<double>> &output_image, int new_width, int new_height)
+{
+    const int oh = (int)input_image.size(), ow = oh ? (int)input_image[0].size() : 0;
+    std::vector<double> in((size_t)ow * oh), out((size_t)new_width * new_height);
+    for (int y = 0; y < oh; y++)
+        for (int x = 0; x < ow; x++) in[(size_t)y * ow + x] = input_image[y][x];
+    pcd_legacy::check(pcd_resize_image(in.data(), ow, oh, out.data(), new_width, new_height), "resize_image");
+    output_image = pcd_legacy::to_rows(out, new_width, new_height);
+}
+
 // main.cpp:111-135
 inline void save_heightmap_as_json(const std::vector<std::vector<double>> &heightmap, const std::string &filename)
 {

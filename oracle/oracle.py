@@ -83,6 +83,9 @@ class Port:
         L.pcdo_sample_vertices.argtypes = [_dp, C.c_int, C.c_int, _dp, C.c_long, C.c_double, C.c_double, _dp]
         L.pcdo_set_source_heights.argtypes = [_dp, _dp, C.c_long]
         L.pcdo_set_source_heights.restype = C.c_double
+        L.pcdo_laplacian_smoothing.argtypes = [_dp, C.c_int, C.c_int, C.c_double]
+        L.pcdo_count_folds.argtypes = [_dp, C.c_int, C.c_int]
+        L.pcdo_count_folds.restype = C.c_long
 
     # solver.cpp:70-148 with one tile (max_threads <= 3)
     def poisson_solver(self, D, phi, max_iterations=100000, tol=1e-7):
@@ -187,6 +190,15 @@ class Port:
         self.L.pcdo_refractive_normals(_f64(inv), _f64(src), n, focal, ri, nx, ny)
         return nx, ny
 
+    def laplacian_smoothing(self, pts, nx, ny, factor):
+        """Mesh::laplacian_smoothing, mesh.cpp:534-606 (returns a smoothed copy)."""
+        p = _f64(pts).copy()
+        self.L.pcdo_laplacian_smoothing(p, int(nx), int(ny), float(factor))
+        return p
+
+    def count_folds(self, pts, nx, ny):
+        return int(self.L.pcdo_count_folds(_f64(pts), int(nx), int(ny)))
+
     def step_grid(self, tgt, vgx, vgy, nx, ny, width, step):
         return self.L.pcdo_step_grid(tgt, _f64(vgx), _f64(vgy), nx, ny, width, step)
 
@@ -282,6 +294,7 @@ class Ref:
         L.ref_design_destroy.argtypes = [C.c_void_p]
         L.ref_save_solid_obj.argtypes = [_dp, _dp, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, C.c_char_p]
         L.ref_export_grid_svg.argtypes = [_dp, C.c_int, C.c_int, C.c_double, C.c_double, C.c_char_p, C.c_double]
+        L.ref_laplacian_smoothing.argtypes = [_dp, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double]
 
     @staticmethod
     def available() -> bool:
@@ -291,6 +304,12 @@ class Ref:
         """save_solid_obj (utils.cpp:198-260) on the structured mesh's triangles."""
         self.L.ref_save_solid_obj(_f64(front), _f64(back), int(nx), int(ny), float(thickness), float(width),
                                   float(height), filename.encode())
+
+    def laplacian_smoothing(self, pts, nx, ny, width, height, factor):
+        """Mesh::laplacian_smoothing (mesh.cpp:534-606) of the reference (a smoothed copy)."""
+        p = _f64(pts).copy()
+        self.L.ref_laplacian_smoothing(p, int(nx), int(ny), float(width), float(height), float(factor))
+        return p
 
     def export_grid_svg(self, pts, nx, ny, width, height, filename, stroke_width):
         """export_grid_to_svg (utils.cpp:262-307)."""

@@ -631,3 +631,63 @@ double pcdo_set_source_heights(double *src, double *hv, long n)
     }
     return s;
 }
+
+/* Mesh::laplacian_smoothing mesh.cpp:534-606 on an nx x ny point set (n x 3):
+ * corners stay; a left/right edge vertex takes the mean y of its three
+ * neighbours (right or left, down, up -- in that order of summation), a
+ * top/bottom edge vertex the mean x of its three (left, right, down / left,
+ * up, right); interior vertices the mean x and y of left, right, up, down;
+ * then p = mean * f + p * (1 - f).  The reference divides by 3.0f / 4.0f
+ * (exact in double) and passes f as a float literal (0.1f). */
+void pcdo_laplacian_smoothing(double *pts, int nx, int ny, double f)
+{
+    long n = (long)nx * ny;
+    double *cp = (double *)malloc(sizeof(double) * 2 * n);
+    for (long i = 0; i < n; i++) {
+        int y = (int)(i / nx), x = (int)(i % nx);
+        double px = pts[3 * i], py = pts[3 * i + 1];
+#define P(yy, xx, c) pts[3 * ((long)(yy) * nx + (xx)) + (c)]
+        int corner = (x == 0 || x == nx - 1) && (y == 0 || y == ny - 1);
+        if (corner) {
+        } else if (x == 0) {
+            py = 0.0; py += P(y, x + 1, 1); py += P(y + 1, x, 1); py += P(y - 1, x, 1); py /= 3.0;
+        } else if (x == nx - 1) {
+            py = 0.0; py += P(y, x - 1, 1); py += P(y - 1, x, 1); py += P(y + 1, x, 1); py /= 3.0;
+        } else if (y == 0) {
+            px = 0.0; px += P(y, x - 1, 0); px += P(y, x + 1, 0); px += P(y + 1, x, 0); px /= 3.0;
+        } else if (y == ny - 1) {
+            px = 0.0; px += P(y, x - 1, 0); px += P(y - 1, x, 0); px += P(y, x + 1, 0); px /= 3.0;
+        } else {
+            px = 0.0; py = 0.0;
+            px += P(y, x - 1, 0); px += P(y, x + 1, 0); px += P(y - 1, x, 0); px += P(y + 1, x, 0);
+            py += P(y, x - 1, 1); py += P(y, x + 1, 1); py += P(y - 1, x, 1); py += P(y + 1, x, 1);
+            px /= 4.0; py /= 4.0;
+        }
+#undef P
+        cp[2 * i] = px;
+        cp[2 * i + 1] = py;
+    }
+    for (long i = 0; i < n; i++) {
+        pts[3 * i] = cp[2 * i] * f + pts[3 * i] * (1.0 - f);
+        pts[3 * i + 1] = cp[2 * i + 1] * f + pts[3 * i + 1] * (1.0 - f);
+    }
+    free(cp);
+}
+
+/* Triangles of the structured mesh (mesh.cpp:57-63) whose signed area is
+ * not positive: folds of the deformed target mesh. */
+long pcdo_count_folds(const double *pts, int nx, int ny)
+{
+    long folds = 0;
+    for (int y = 0; y < ny - 1; y++)
+        for (int x = 0; x < nx - 1; x++) {
+            long i = (long)y * nx + x;
+            long t[2][3] = {{i, i + 1, i + nx}, {i + nx, i + 1, i + nx + 1}};
+            for (int k = 0; k < 2; k++) {
+                const double *a = pts + 3 * t[k][0], *b = pts + 3 * t[k][1], *c = pts + 3 * t[k][2];
+                double area2 = (b[0] - a[0]) * (c[1] - a[1]) - (c[0] - a[0]) * (b[1] - a[1]);
+                if (!(area2 > 0.0)) folds++;
+            }
+        }
+    return folds;
+}

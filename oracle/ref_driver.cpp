@@ -157,6 +157,18 @@ void ref_export_grid_svg(const double *pts, int nx, int ny, double width, double
     export_grid_to_svg(P, width, height, nx, ny, std::string(filename), stroke_width);
 }
 
+// Mesh::laplacian_smoothing, mesh.cpp:534-606 (public member), in place on
+// an nx*ny x 3 point set.
+void ref_laplacian_smoothing(double *pts, int nx, int ny, double width, double height, double factor)
+{
+    Mesh m(width, height, nx, ny);
+    std::vector<point_t> P;
+    for (int i = 0; i < nx * ny; i++) P.push_back({pts[3 * i], pts[3 * i + 1], pts[3 * i + 2]});
+    m.laplacian_smoothing(P, factor);
+    for (int i = 0; i < nx * ny; i++)
+        for (int c = 0; c < 3; c++) pts[3 * i + c] = P[i][c];
+}
+
 void ref_design_destroy(void *h)
 {
     auto *d = static_cast<Caustic_design *>(h);

@@ -23,6 +23,7 @@ PCD_TIMEOUT = 4
 PCD_RASTER_MISS = 5
 PCD_NO_DEVICE = 6
 PCD_FALLBACK_USED = 7
+PCD_MESH_SMOOTHED = 8
 
 STOP_MAX_UPDATE = 0
 STOP_REL_RESIDUAL = 1
@@ -96,6 +97,7 @@ class DesignParams(C.Structure):
         ("thickness", C.c_double),
         ("transport", SolveOpts),
         ("height_solve", SolveOpts),
+        ("raster_miss_policy", C.c_int),
     ]
 
 
@@ -140,6 +142,13 @@ SIGNATURES = {
     "pcd_design_export_parameterization_svg": (C.c_int, [_vp, C.c_char_p, C.c_double]),
     "pcd_design_export_inverted_transport_map_svg": (C.c_int, [_vp, C.c_char_p, C.c_double]),
     "pcd_design_save_heightmap_json": (C.c_int, [_vp, C.c_char_p]),
+    "pcd_design_smooth_target_mesh": (C.c_int, [_vp, C.c_double]),
+    "pcd_image_to_grid": (C.c_int, [C.c_char_p, C.POINTER(C.c_int), C.POINTER(C.c_int), _dp]),
+    "pcd_png_decode": (C.c_int, [C.c_char_p, C.c_size_t, C.POINTER(C.c_int), C.POINTER(C.c_int), C.c_char_p]),
+    "pcd_resize_image": (C.c_int, [_dp, C.c_int, C.c_int, _dp, C.c_int, C.c_int]),
+    "pcd_resize_image_device": (C.c_int, [_vp, _vp, C.c_int, C.c_int, C.c_int, _vp, C.c_int, C.c_int, C.c_int, _vp]),
+    "pcd_design_count_folds": (C.c_int, [_vp, C.POINTER(C.c_longlong)]),
+    "pcd_design_set_target_points": (C.c_int, [_vp, _dp]),
     "pcd_ctx_autotune_info": (C.c_int, [_vp, C.POINTER(C.c_int), C.POINTER(C.c_longlong)]),
     "pcd_gradient_device": (C.c_int, [_vp, _vp, _vp, _vp, C.c_int, C.c_int, _vp]),
     "pcd_divergence_device": (C.c_int, [_vp, _vp, _vp, _vp, C.c_int, C.c_int, _vp]),

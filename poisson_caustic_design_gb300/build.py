@@ -20,7 +20,10 @@ LIB = os.path.join(OUT_DIR, "libpcd_gb300.so")
 INCLUDE = os.path.join(ROOT, "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+# host code: no floating-point contraction, so host arithmetic (the image gray
+# conversion, the writers' inputs) gives the same bits on x86-64 and aarch64
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall",
+              "-Xcompiler", "-ffp-contract=off",
               "--expt-relaxed-constexpr", "-I" + INCLUDE]
 
 

@@ -36,7 +36,7 @@ VERT = {"target_points": 10, "source_points": 11, "target_areas": 12, "errors": 
 
 class CausticDesign:
     def __init__(self, ctx: Context | None = None, transport: SolveOptions | None = None,
-                 height_solve: SolveOptions | None = None):
+                 height_solve: SolveOptions | None = None, raster_miss_policy: int = 0):
         self._L = _lib.load()
         self._ctx = ctx or Context()
         self._own_ctx = ctx is None
@@ -49,6 +49,10 @@ class CausticDesign:
         self.transport_opts = transport or SolveOptions(tol=1e-7)      # caustic_design.cpp:222
         self.height_opts = height_solve or SolveOptions(tol=1e-8)      # caustic_design.cpp:311
         self.last_solve_stats = None
+        # 0: a raster miss raises PCDError (PCD_RASTER_MISS; the reference
+        # exits); 1: the target mesh is smoothed and the iteration returns NaN
+        self.raster_miss_policy = int(raster_miss_policy)
+        self.last_status = None
 
     # ---- setters (caustic_design.cpp:28-53) ----
     def set_mesh_resolution(self, width: int, height: int):
@@ -83,18 +87,40 @@ class CausticDesign:
         p.focal_l, p.thickness = self.focal_l, self.thickness
         p.transport = self.transport_opts.to_c()
         p.height_solve = self.height_opts.to_c()
+        p.raster_miss_policy = self.raster_miss_policy
         h = C.c_void_p()
         check(self._L.pcd_design_create(self._ctx.handle, C.byref(p), C.byref(h)), "pcd_design_create")
         self._h = h
         check(self._L.pcd_design_initialize(self._h, img.ctypes.data), "pcd_design_initialize")
 
     def perform_transport_iteration(self) -> float:
+        """Returns the step size; NaN when a raster miss was handled by
+        smoothing the target mesh (raster_miss_policy 1, status in
+        ``last_status``), as caustic_design.cpp:214-217 intends."""
         step = C.c_double(0)
         st = _lib.SolveStats()
-        check(self._L.pcd_design_transport_iteration(self._h, C.byref(step), C.byref(st)),
-              "pcd_design_transport_iteration")
+        self.last_status = check(self._L.pcd_design_transport_iteration(self._h, C.byref(step), C.byref(st)),
+                                 "pcd_design_transport_iteration", (_lib.PCD_OK, _lib.PCD_MESH_SMOOTHED))
         self.last_solve_stats = st.as_dict()
         return step.value
+
+    # ---- fold handling ----
+    def smooth_target_mesh(self, smoothing_factor: float):
+        """Mesh::laplacian_smoothing (mesh.cpp:534-606) of the target mesh."""
+        check(self._L.pcd_design_smooth_target_mesh(self._h, float(smoothing_factor)), "smooth_target_mesh")
+
+    def count_folds(self) -> int:
+        """Triangles of the target mesh with non-positive signed area."""
+        n = C.c_longlong(0)
+        check(self._L.pcd_design_count_folds(self._h, C.byref(n)), "count_folds")
+        return n.value
+
+    def set_target_points(self, points):
+        p = np.ascontiguousarray(points, dtype=np.float64)
+        if p.shape != (self.mesh_res_x * self.mesh_res_y, 3):
+            raise ValueError("points must be mesh_res_x * mesh_res_y x 3")
+        check(self._L.pcd_design_set_target_points(self._h, p.ctypes.data_as(C.POINTER(C.c_double))),
+              "set_target_points")
 
     def perform_height_map_iteration(self, itr: int = 0) -> float:
         upd = C.c_double(0)

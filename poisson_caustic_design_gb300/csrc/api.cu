@@ -1,6 +1,7 @@
 // api.cu -- C ABI of libpcd_gb300: context, Poisson solve, grid utilities.
 //
 // Declarations and the reference interfaces they replace: include/pcd.h.
+#include <algorithm>
 #include <atomic>
 #include <cstdio>
 #include <cstring>
@@ -131,6 +132,7 @@ const char *pcd_status_string(int status)
     case PCD_RASTER_MISS: return "raster miss";
     case PCD_NO_DEVICE: return "no CUDA device";
     case PCD_FALLBACK_USED: return "fallback used";
+    case PCD_MESH_SMOOTHED: return "raster miss: target mesh smoothed";
     }
     return "unknown status";
 }
@@ -280,6 +282,24 @@ int pcd_poisson_solver(const double *D, double *phi, int width, int height, int 
     return pcd_poisson_solve(ctx, D, phi, width, height, &o, nullptr);
 }
 
+int pcd_resize_image(const double *in, int old_width, int old_height, double *out, int new_width, int new_height)
+{
+    if (!in || !out || old_width < 1 || old_height < 1 || new_width < 1 || new_height < 1) return PCD_BAD_ARG;
+    pcd_ctx *ctx = nullptr;
+    PCD_TRY(default_ctx(&ctx));
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    PCD_TRY(ctx_activate(ctx));
+    const size_t ni = (size_t)old_width * old_height, no = (size_t)new_width * new_height;
+    PCD_TRY(ctx_stage(ctx, std::max(ni, no)));
+    cudaStream_t s = ctx->stream;
+    PCD_CUDA(cudaMemcpyAsync(ctx->d_b, in, ni * sizeof(double), cudaMemcpyHostToDevice, s));
+    PCD_TRY(resize_nearest(ctx->d_b, old_width, old_height, old_width, ctx->d_phi, new_width, new_height, new_width,
+                           s));
+    PCD_CUDA(cudaMemcpyAsync(out, ctx->d_phi, no * sizeof(double), cudaMemcpyDeviceToHost, s));
+    PCD_CUDA(cudaStreamSynchronize(s));
+    return PCD_OK;
+}
+
 int pcd_batch_solve_device(pcd_ctx *ctx, const pcd_instance *inst, int count, const pcd_solve_opts *opts,
                            pcd_instance_stats *stats, pcd_batch_stats *batch_stats, void *stream)
 {
@@ -320,6 +340,20 @@ int pcd_gradient_device(pcd_ctx *ctx, const double *g, double *gx, double *gy, i
     StreamJoin j(ctx, stream);
     PCD_TRY(j.begin());
     PCD_TRY(gradient(g, gx, gy, width, height, j.work));
+    return j.end();
+}
+
+int pcd_resize_image_device(pcd_ctx *ctx, const double *in, int old_width, int old_height, int in_ld, double *out,
+                            int new_width, int new_height, int out_ld, void *stream)
+{
+    if (!ctx || !in || !out || old_width < 1 || old_height < 1 || new_width < 1 || new_height < 1 ||
+        in_ld < old_width || out_ld < new_width)
+        return PCD_BAD_ARG;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    PCD_TRY(ctx_activate(ctx));
+    StreamJoin j(ctx, stream);
+    PCD_TRY(j.begin());
+    PCD_TRY(resize_nearest(in, old_width, old_height, in_ld, out, new_width, new_height, out_ld, j.work));
     return j.end();
 }
 

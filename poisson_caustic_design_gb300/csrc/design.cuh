@@ -44,6 +44,9 @@ struct Design {
     int height_iteration(int itr, double *update_out, pcd_solve_stats *stats);
     int get_grid(int which, double *out);
     int get_vertices(int which, double *out);
+    int smooth_target(double f);
+    int count_folds(long long *folds);
+    int set_target_points(const double *pts3);
 
    private:
     int locate(const double2 *pts, int mode, int qx, int qy, cudaStream_t s);

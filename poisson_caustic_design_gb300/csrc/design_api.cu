@@ -124,4 +124,34 @@ int pcd_design_get_vertices(pcd_design *d, int which, double *host_out)
     return d->d.get_vertices(which, host_out);
 }
 
+int pcd_design_smooth_target_mesh(pcd_design *d, double smoothing_factor)
+{
+    if (!d) return PCD_BAD_ARG;
+    PCD_TRY(live(d));
+    std::lock_guard<std::mutex> lk(d->d.ctx->mu);
+    PCD_TRY(ctx_activate(d->d.ctx));
+    if (!d->d.initialized) return PCD_BAD_ARG;
+    return d->d.smooth_target(smoothing_factor);
+}
+
+int pcd_design_count_folds(pcd_design *d, long long *folds)
+{
+    if (!d || !folds) return PCD_BAD_ARG;
+    PCD_TRY(live(d));
+    std::lock_guard<std::mutex> lk(d->d.ctx->mu);
+    PCD_TRY(ctx_activate(d->d.ctx));
+    if (!d->d.initialized) return PCD_BAD_ARG;
+    return d->d.count_folds(folds);
+}
+
+int pcd_design_set_target_points(pcd_design *d, const double *points)
+{
+    if (!d || !points) return PCD_BAD_ARG;
+    PCD_TRY(live(d));
+    std::lock_guard<std::mutex> lk(d->d.ctx->mu);
+    PCD_TRY(ctx_activate(d->d.ctx));
+    if (!d->d.initialized) return PCD_BAD_ARG;
+    return d->d.set_target_points(points);
+}
+
 }  // extern "C"

@@ -97,7 +97,21 @@ __global__ void __launch_bounds__(kT) k_divergence(const double *__restrict__ nx
     }
 }
 
+// resize_image, main.cpp:13-27: nearest sample at integer source indices
+// x * old_width / new_width, y * old_height / new_height.
+__global__ void __launch_bounds__(kT) k_resize_nearest(const double *__restrict__ in, int ow, int oh, int ild,
+                                                       double *__restrict__ out, int nw, int nh, int old)
+{
+    const long n = (long)nw * nh;
+    for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x) {
+        const int y = (int)(t / nw), x = (int)(t - (long)y * nw);
+        const int sx = (int)((long)x * ow / nw), sy = (int)((long)y * oh / nh);
+        out[(long)y * old + x] = in[(long)sy * ild + sx];
+    }
+}
+
 inline int blocks_for(long n) { return (int)std::min<long>(kBlocks, (n + kT - 1) / kT); }
+
 }  // namespace
 
 int GridScratch::reserve()
@@ -133,6 +147,13 @@ int subtract_average(GridScratch &sc, double *g, long n, cudaStream_t s)
 int gradient(const double *g, double *gx, double *gy, int W, int H, cudaStream_t s)
 {
     k_gradient<<<blocks_for((long)W * H), kT, 0, s>>>(g, gx, gy, W, H);
+    PCD_LAUNCHED(1);
+    return PCD_OK;
+}
+
+int resize_nearest(const double *in, int ow, int oh, int ild, double *out, int nw, int nh, int old, cudaStream_t s)
+{
+    k_resize_nearest<<<blocks_for((long)nw * nh), kT, 0, s>>>(in, ow, oh, ild, out, nw, nh, old);
     PCD_LAUNCHED(1);
     return PCD_OK;
 }

@@ -17,5 +17,6 @@ struct GridScratch {
 int subtract_average(GridScratch &sc, double *g, long n, cudaStream_t s);
 int gradient(const double *g, double *gx, double *gy, int W, int H, cudaStream_t s);
 int divergence(const double *nx, const double *ny, double *div, int W, int H, cudaStream_t s);
+int resize_nearest(const double *in, int ow, int oh, int ild, double *out, int nw, int nh, int old, cudaStream_t s);
 
 }  // namespace pcd

@@ -595,6 +595,67 @@ __global__ void k_points_out(const double2 *xy, const double *z, int nx, int ny,
     }
 }
 
+// Mesh::laplacian_smoothing mesh.cpp:534-606, pass 1: the neighbour means
+// (same summation order as the reference) into `mean`.
+__global__ void k_smooth_mean(const double2 *__restrict__ tp, int nx, int ny, double2 *__restrict__ mean)
+{
+    const int n = nx * ny;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const int y = i / nx, x = i - y * nx;
+        double2 q = tp[i];
+        const bool corner = (x == 0 || x == nx - 1) && (y == 0 || y == ny - 1);
+        if (corner) {
+        } else if (x == 0) {
+            q.y = ((0.0 + tp[i + 1].y) + tp[i + nx].y) + tp[i - nx].y;
+            q.y /= 3.0;
+        } else if (x == nx - 1) {
+            q.y = ((0.0 + tp[i - 1].y) + tp[i - nx].y) + tp[i + nx].y;
+            q.y /= 3.0;
+        } else if (y == 0) {
+            q.x = ((0.0 + tp[i - 1].x) + tp[i + 1].x) + tp[i + nx].x;
+            q.x /= 3.0;
+        } else if (y == ny - 1) {
+            q.x = ((0.0 + tp[i - 1].x) + tp[i - nx].x) + tp[i + 1].x;
+            q.x /= 3.0;
+        } else {
+            q.x = (((0.0 + tp[i - 1].x) + tp[i + 1].x) + tp[i - nx].x) + tp[i + nx].x;
+            q.y = (((0.0 + tp[i - 1].y) + tp[i + 1].y) + tp[i - nx].y) + tp[i + nx].y;
+            q.x /= 4.0;
+            q.y /= 4.0;
+        }
+        mean[i] = q;
+    }
+}
+
+// pass 2: p = mean * f + p * (1 - f)
+__global__ void k_smooth_apply(double2 *__restrict__ tp, const double2 *__restrict__ mean, int n, double f)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const double2 m = mean[i], p = tp[i];
+        tp[i] = make_double2(__dadd_rn(__dmul_rn(m.x, f), __dmul_rn(p.x, 1.0 - f)),
+                             __dadd_rn(__dmul_rn(m.y, f), __dmul_rn(p.y, 1.0 - f)));
+    }
+}
+
+// triangles {i, i+1, i+nx}, {i+nx, i+1, i+nx+1} (mesh.cpp:57-63) with signed area <= 0
+__global__ void k_count_folds(const double2 *__restrict__ tp, int nx, int ny, unsigned long long *count)
+{
+    unsigned long long local = 0;
+    const long nq = (long)(nx - 1) * (ny - 1);
+    for (long q = (long)blockIdx.x * blockDim.x + threadIdx.x; q < nq; q += (long)gridDim.x * blockDim.x) {
+        const int y = (int)(q / (nx - 1)), x = (int)(q - (long)y * (nx - 1));
+        const long i = (long)y * nx + x;
+        const long t[2][3] = {{i, i + 1, i + nx}, {i + nx, i + 1, i + nx + 1}};
+        for (int k = 0; k < 2; k++) {
+            const double2 a = tp[t[k][0]], b = tp[t[k][1]], c = tp[t[k][2]];
+            const double area2 = __dsub_rn(__dmul_rn(b.x - a.x, c.y - a.y), __dmul_rn(c.x - a.x, b.y - a.y));
+            if (!(area2 > 0.0)) local++;
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) local += __shfl_xor_sync(0xffffffffu, local, o);
+    if ((threadIdx.x & 31) == 0 && local) atomicAdd(count, local);
+}
+
 }  // namespace
 
 // ---------------------------------------------------------------------------
@@ -710,8 +771,14 @@ int Design::transport_iteration(double *step_out, pcd_solve_stats *stats)
     unsigned int misses = 0;
     PCD_TRY(raster_values(tp, errors, nullptr, raster, nullptr, s, &misses));
     if (misses) {
-        set_error("raster miss: " + std::to_string(misses) + " grid samples outside every triangle");
         if (step_out) *step_out = NAN;
+        if (p.raster_miss_policy == 1) {
+            // caustic_design.cpp:214-217 (unreached in the reference, which
+            // exits first): smooth the target mesh with the float literal 0.1f
+            PCD_TRY(smooth_target((double)0.1f));
+            return PCD_MESH_SMOOTHED;
+        }
+        set_error("raster miss: " + std::to_string(misses) + " grid samples outside every triangle");
         return PCD_RASTER_MISS;
     }
     // subtractAverage + poisson_solver (caustic_design.cpp:221-222)
@@ -788,6 +855,42 @@ int Design::height_iteration(int itr, double *update_out, pcd_solve_stats *stats
     double u;
     std::memcpy(&u, small_host + 2, sizeof(double));
     if (update_out) *update_out = u;
+    return PCD_OK;
+}
+
+int Design::smooth_target(double f)
+{
+    cudaStream_t s = ctx->stream;
+    const int nx = p.mesh_res_x, ny = p.mesh_res_y, nv = nx * ny;
+    k_smooth_mean<<<nblocks(nv), kT, 0, s>>>(tp, nx, ny, inv);  // inv: scratch, recomputed on use
+    PCD_LAUNCHED(1);
+    k_smooth_apply<<<nblocks(nv), kT, 0, s>>>(tp, inv, nv, f);
+    PCD_LAUNCHED(1);
+    PCD_CUDA(cudaStreamSynchronize(s));
+    return PCD_OK;
+}
+
+int Design::count_folds(long long *folds)
+{
+    cudaStream_t s = ctx->stream;
+    const int nx = p.mesh_res_x, ny = p.mesh_res_y;
+    unsigned long long *cnt = small + 2;
+    PCD_CUDA(cudaMemsetAsync(cnt, 0, sizeof(unsigned long long), s));
+    k_count_folds<<<nblocks((long)(nx - 1) * (ny - 1)), kT, 0, s>>>(tp, nx, ny, cnt);
+    PCD_LAUNCHED(1);
+    PCD_CUDA(cudaMemcpyAsync(small_host + 3, cnt, sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+    PCD_CUDA(cudaStreamSynchronize(s));
+    *folds = (long long)small_host[3];
+    return PCD_OK;
+}
+
+int Design::set_target_points(const double *pts3)
+{
+    const int nv = p.mesh_res_x * p.mesh_res_y;
+    std::vector<double2> h((size_t)nv);
+    for (int i = 0; i < nv; i++) h[(size_t)i] = make_double2(pts3[3 * i], pts3[3 * i + 1]);
+    PCD_CUDA(cudaMemcpyAsync(tp, h.data(), sizeof(double2) * nv, cudaMemcpyHostToDevice, ctx->stream));
+    PCD_CUDA(cudaStreamSynchronize(ctx->stream));
     return PCD_OK;
 }
 

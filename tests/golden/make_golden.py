@@ -14,6 +14,8 @@ Fixtures (all float64, seeded inputs, the reference run with max_threads=1):
   export_grid_to_svg (utils.cpp:262-307) output files (bytes) of the
   reference on seeded point sets: ragged and square meshes, negative heights,
   %g exponents, the non-square SVG whose second loop uses res_x as bound.
+* mesh_cases.npz -- Mesh::laplacian_smoothing (mesh.cpp:534-606) with the
+  factor 0.1f of caustic_design.cpp:216 on perturbed meshes (one folded).
 * pipeline_r{16,32,64}.npz -- Caustic_design replay of main.cpp:216-262 at
   mesh resolution r (grid 4r): per-iteration step sizes, target areas, the
   first iteration's errors/raster, final phi / target points, and after the
@@ -150,12 +152,27 @@ def writer_cases(R: O.Ref):
     np.savez_compressed(os.path.join(OUT, "writer_cases.npz"), **cases)
 
 
+def mesh_cases(R: O.Ref):
+    rng = np.random.default_rng(31)
+    cases = {}
+    f = float(np.float32(0.1))
+    for name, nx, ny, w, h, sig in (("smooth_a", 9, 7, 0.5, 0.35, 0.02), ("smooth_b", 16, 16, 0.5, 0.5, 0.06)):
+        y, x = np.meshgrid(np.arange(ny) * h / (ny - 1), np.arange(nx) * w / (nx - 1), indexing="ij")
+        p = np.stack([x.ravel(), y.ravel(), np.zeros(nx * ny)], axis=1)
+        p[:, :2] += rng.normal(0, sig * w / nx, (nx * ny, 2))
+        cases[f"{name}/points"] = p
+        cases[f"{name}/params"] = np.array([nx, ny, w, h, f])
+        cases[f"{name}/smoothed"] = R.laplacian_smoothing(p, nx, ny, w, h, f)
+    np.savez_compressed(os.path.join(OUT, "mesh_cases.npz"), **cases)
+
+
 def main():
     O.build(ref=True)
     R = O.Ref()
     solver_cases(R)
     utils_cases(R)
     writer_cases(R)
+    mesh_cases(R)
     for res, seed in ((16, 3), (32, 11), (64, 29)):
         n = pipeline(R, res, seed)
         print(f"pipeline r{res}: {n} transport iterations")

@@ -133,3 +133,22 @@ def test_threaded_port_matches_reference_schedule(port):
     phi = np.zeros_like(b)
     port.poisson_solver_threads(b, phi, 100000, 1e-7, 16)
     assert oracle.rel_err_mod_const(phi, ref)[0] < 1e-7
+
+
+@pytest.mark.parametrize("name", ["smooth_a", "smooth_b"])
+def test_laplacian_smoothing_port_matches_reference(port, name):
+    """Mesh::laplacian_smoothing (mesh.cpp:534-606), factor 0.1f: the port is
+    bit-identical to the reference's compiled function (golden)."""
+    z = load_golden("mesh_cases.npz")
+    nx, ny, w, h, f = z[f"{name}/params"]
+    out = port.laplacian_smoothing(z[f"{name}/points"], int(nx), int(ny), f)
+    assert np.array_equal(out, z[f"{name}/smoothed"])
+
+
+def test_fold_count_port(port):
+    nx = ny = 8
+    y, x = np.meshgrid(np.arange(ny) / (ny - 1), np.arange(nx) / (nx - 1), indexing="ij")
+    p = np.stack([x.ravel(), y.ravel(), np.zeros(nx * ny)], axis=1)
+    assert port.count_folds(p, nx, ny) == 0
+    p[3 * nx + 3, 0] += 1.6 / (nx - 1)   # past its right neighbour: its fan inverts
+    assert port.count_folds(p, nx, ny) > 0

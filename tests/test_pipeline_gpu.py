@@ -154,3 +154,61 @@ def test_design_output_files(ctx, port, tmp_path):
     assert miss == 0
     np.testing.assert_allclose(inv[:, :2], ref_inv, rtol=0, atol=1e-12)
     d.close()
+
+
+def test_fold_handling(ctx, port):
+    """Fold handling (no counterpart in the reference, which exits on a raster
+    miss): the device Laplacian smoothing equals the reference's
+    Mesh::laplacian_smoothing bit for bit (golden), the fold count equals the
+    port's, and a raster miss either raises PCD_RASTER_MISS (policy 0) or
+    smooths the target mesh and returns NaN (policy 1)."""
+    import poisson_caustic_design_gb300 as pcd
+
+    z = load_golden("pipeline_r16.npz")
+    m = load_golden("mesh_cases.npz")
+    d, _ = _design(ctx, z)
+    nx, ny, w, h, f = m["smooth_b/params"]
+    assert int(nx) == d.mesh_res_x and float(w) == d.width
+    d.set_target_points(m["smooth_b/points"])
+    d.smooth_target_mesh(f)
+    assert np.array_equal(d.target_points()[:, :2], m["smooth_b/smoothed"][:, :2])
+    # a planted fold
+    r = d.mesh_res_x
+    p = d.target_points().copy()
+    p[5 * r + 5, 0] += 1.6 * d.width / (r - 1)
+    d.set_target_points(p)
+    assert d.count_folds() == port.count_folds(p, r, r) > 0
+    # a bottom-edge vertex pulled inward leaves grid samples outside every triangle
+    y0, x0 = np.meshgrid(np.arange(r) * d.height / (r - 1), np.arange(r) * d.width / (r - 1), indexing="ij")
+    flat = np.stack([x0.ravel(), y0.ravel(), np.zeros(r * r)], axis=1)
+    notch = flat.copy()
+    notch[7, 1] += 0.3 * d.height
+    d.set_target_points(notch)
+    with pytest.raises(pcd.PCDError) as e:
+        d.perform_transport_iteration()
+    assert e.value.status == pcd._lib.PCD_RASTER_MISS
+    d.close()
+    d2 = pcd.CausticDesign(ctx, raster_miss_policy=1)
+    r_, width, focal, thickness, conv, seed = z["params"]
+    d2.set_mesh_resolution(r, r)
+    d2.set_domain_resolution(4 * r, 4 * r)
+    d2.set_mesh_size(width, width)
+    d2.set_lens_focal_length(focal)
+    d2.set_lens_thickness(thickness)
+    d2.initialize_solvers(z["image"])
+    d2.set_target_points(notch)
+    s = d2.perform_transport_iteration()
+    assert np.isnan(s) and d2.last_status == pcd._lib.PCD_MESH_SMOOTHED
+    expect = port.laplacian_smoothing(notch, r, r, float(np.float32(0.1)))
+    assert np.array_equal(d2.target_points()[:, :2], expect[:, :2])
+    d2.close()
+
+
+@pytest.mark.parametrize("ow,oh,nw,nh", [(128, 128, 512, 512), (37, 53, 100, 61), (640, 480, 64, 64)])
+def test_resize_image_matches_port(port, ow, oh, nw, nh):
+    """resize_image (main.cpp:13-27) on the GPU: bit-identical to the port."""
+    from poisson_caustic_design_gb300 import image
+
+    img = np.random.default_rng(ow + nh).random((oh, ow))
+    got = image.resize_image(img, nw, nh)
+    assert np.array_equal(got, port.resize_nearest(img, nw, nh))
