@@ -151,9 +151,11 @@ class CausticDesign:
         check(self._L.pcd_design_get_grid(self._h, GRID[name], out.ctypes.data), "pcd_design_get_grid")
         return out
 
+    _POINT_FIELDS = ("target_points", "source_points", "inverted_map")  # n x 3
+
     def _vert(self, name):
         n = self.mesh_res_x * self.mesh_res_y
-        out = np.empty((n, 3)) if name.endswith("points") else np.empty(n)
+        out = np.empty((n, 3)) if name in self._POINT_FIELDS else np.empty(n)
         check(self._L.pcd_design_get_vertices(self._h, VERT[name], out.ctypes.data), "pcd_design_get_vertices")
         return out
 
@@ -179,6 +181,10 @@ class CausticDesign:
 
     def source_points(self):
         return self._vert("source_points")
+
+    def inverted_map(self):
+        """The inverted transport map of the current target mesh (mesh.cpp:348-409), n x 3 with z = 0."""
+        return self._vert("inverted_map")
 
     def close(self):
         if self._h:

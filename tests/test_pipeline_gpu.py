@@ -142,7 +142,7 @@ def test_design_output_files(ctx, port, tmp_path):
     same(d.save_solid_obj_target, lambda f: pcd.save_solid_obj(tp, sp, r, r, d.thickness, d.width, d.height, f))
     same(lambda f: d.export_paramererization_to_svg(f, 0.5),
          lambda f: pcd.export_grid_to_svg(tp, d.width, d.height, r, r, f, 0.5))
-    inv = d._vert("inverted_map")
+    inv = d.inverted_map()
     same(lambda f: d.export_inverted_transport_map(f, 1.0),
          lambda f: pcd.export_grid_to_svg(inv, d.width, d.height, r, r, f, 1.0))
     a = tmp_path / "hj"
