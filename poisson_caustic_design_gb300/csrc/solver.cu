@@ -814,7 +814,7 @@ namespace {
 // next cycle is launched before the previous one's control block is read; a
 // cycle launched after convergence returns at once.
 int solve_cluster(SolverWorkspace &ws, const double *b, double *phi, const SolveArgs &a, const pcd_solve_opts &o,
-                  int C, size_t smem, int khp, int depth, pcd_solve_stats *stats, cudaStream_t s)
+                  const ClusterPlan &plan, pcd_solve_stats *stats, cudaStream_t s)
 {
     const int rblocks = grid_blocks((long)a.W * a.H);
     PCD_CUDA(cudaMemsetAsync(ws.e32, 0, sizeof(float) * (size_t)a.H * a.ld, s));
@@ -825,7 +825,7 @@ int solve_cluster(SolverWorkspace &ws, const double *b, double *phi, const Solve
     PCD_LAUNCHED(1);
 
     ClusterArgs ca{};
-    ca.W = a.W; ca.H = a.H; ca.ld = a.ld; ca.khp = khp;
+    ca.W = a.W; ca.H = a.H; ca.ld = a.ld; ca.khp = plan.khp;
     ca.e = ws.e32; ca.r32 = ws.r32; ca.ctl = ws.ctl;
     ca.check_every = o.check_every > 0 ? o.check_every : 16;
     ca.cycle_cap = o.refine_every > 0 ? o.refine_every : 2048;
@@ -834,7 +834,7 @@ int solve_cluster(SolverWorkspace &ws, const double *b, double *phi, const Solve
     ca.drop = o.refine_drop > 0.0 ? o.refine_drop : 3e-2;
     for (int c = 0; c < 5; c++) ca.w32[c] = a.w32[c];
     ca.one_minus_omega = (float)(1.0 - a.omega);
-    ca.depth = depth;
+    ca.depth = plan.depth;
 
     PCD_CUDA(cudaEventRecord(ws.k0, s));
     long launched = 0;
@@ -845,7 +845,7 @@ int solve_cluster(SolverWorkspace &ws, const double *b, double *phi, const Solve
             set_error("cluster SOR: cycle budget exceeded without a done flag");
             return PCD_TIMEOUT;
         }
-        PCD_TRY(launch_cluster(ca, C, smem, s));
+        PCD_TRY(launch_cluster(ca, plan, s));
         k_refine_residual<false><<<rblocks, kThreads, 0, s>>>(phi, ws.e32, b, ws.mask, ws.r32, ws.ctl, ws.partials, a, 0);
         PCD_LAUNCHED(1);
         k_refine_update<<<rblocks, kThreads, 0, s>>>(phi, ws.e32, ws.ctl, a);
@@ -990,10 +990,8 @@ int solve_device(SolverWorkspace &ws, const double *b, double *phi, int W, int H
 
     if (!done_already && !masked && precision == PCD_PREC_MIXED && a.stop == PCD_STOP_REL_RESIDUAL &&
         (o.schedule == PCD_SCHED_AUTO || o.schedule == PCD_SCHED_CLUSTER)) {
-        int C = 0, khp = 0, depth = 0;
-        size_t smem = 0;
-        if (cluster_plan(ws.dev, W, H, 2, &C, &smem, &khp, &depth) == PCD_OK)
-            return solve_cluster(ws, b, phi, a, o, C, smem, khp, depth, stats, s);
+        ClusterPlan plan{};
+        if (cluster_plan(ws.dev, W, H, 4, &plan) == PCD_OK) return solve_cluster(ws, b, phi, a, o, plan, stats, s);
     }
     if (!done_already && !masked &&
         (o.schedule == PCD_SCHED_AUTO || o.schedule == PCD_SCHED_PERSISTENT || o.schedule == PCD_SCHED_CLUSTER)) {

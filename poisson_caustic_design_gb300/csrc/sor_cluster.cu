@@ -148,12 +148,24 @@ __host__ __device__ inline size_t tb_floats(int nmax, int KHp)
     return (size_t)4 * (nmax + 2 * HK) * KHp + (size_t)8 * HK * KHp;
 }
 
-// Colour c on plane rows [lo, hi) intersected with the thread's row block
-// [rb0, rb1), walked top-down: the other colour's rows lr-1, lr, lr+1 stay in
-// registers from one row to the next (one new 16-byte load of them per row).
-// With SHFL (a warp lies within one row group and its lanes hold consecutive
-// quads) the neighbour one slot beyond the quad comes from the adjacent lane;
-// the first / last lane of the warp load it.
+__device__ __forceinline__ float4 lds4(unsigned a)
+{
+    float4 v;
+    asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];" : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w) : "r"(a));
+    return v;
+}
+__device__ __forceinline__ float lds1(unsigned a)
+{
+    float v;
+    asm volatile("ld.shared.f32 %0, [%1];" : "=f"(v) : "r"(a));
+    return v;
+}
+__device__ __forceinline__ void sts4(unsigned a, const float4 &v)
+{
+    asm volatile("st.shared.v4.f32 [%0], {%1, %2, %3, %4};" ::"r"(a), "f"(v.x), "f"(v.y), "f"(v.z), "f"(v.w)
+                 : "memory");
+}
+
 // The first / last quad of an interior row after the interior form: the
 // cell at x = 0 lacks its left neighbour, the one at x = W-1 its right one
 // (three neighbours, both when W = 1), cells past the last column keep v.
@@ -181,32 +193,18 @@ __device__ __forceinline__ float4 quad_edge_fix(float4 nv, const float4 &v, cons
     return make_float4(out[0], out[1], out[2], out[3]);
 }
 
-__device__ __forceinline__ float4 lds4(unsigned a)
-{
-    float4 v;
-    asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];" : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w) : "r"(a));
-    return v;
-}
-__device__ __forceinline__ float lds1(unsigned a)
-{
-    float v;
-    asm volatile("ld.shared.f32 %0, [%1];" : "=f"(v) : "r"(a));
-    return v;
-}
-__device__ __forceinline__ void sts4(unsigned a, const float4 &v)
-{
-    asm volatile("st.shared.v4.f32 [%0], {%1, %2, %3, %4};" ::"r"(a), "f"(v.x), "f"(v.y), "f"(v.z), "f"(v.w)
-                 : "memory");
-}
-
-template <bool SHFL>
+// Colour c on plane rows [lo, hi) intersected with the thread's row block
+// [rb0, rb1), walked top-down: the other colour's rows lr-1, lr, lr+1 stay in
+// registers from one row to the next (one new 16-byte load of them per row),
+// the neighbour one slot beyond the quad is a 4-byte load.  Any width; the
+// first and last quads of a row take the edge fix-up, the grid's first and
+// last rows the general form.
 __device__ __forceinline__ void tb_relax_block(float *own_p, const float *oth_p, const float *rhs_p, int c, int lo,
                                                int hi, int rb0, int rb1, int ybase, const Grid &G, int KHp, int k)
 {
     const int W = G.W, H = G.H;
     const float w4 = G.w4, w3 = G.w3, w2 = G.w2;
     const int l0 = max(lo, rb0), l1 = min(hi, rb1);
-    const int lane = threadIdx.x & 31;
     // 32-bit shared-memory addresses of slot k of row 0 of each plane
     const unsigned row_bytes = 4u * (unsigned)KHp;
     const unsigned own = (unsigned)__cvta_generic_to_shared(own_p) + 4u * k;
@@ -225,14 +223,7 @@ __device__ __forceinline__ void tb_relax_block(float *own_p, const float *oth_p,
         dn = lds4(oth + ro + row_bytes);
         const int y = ybase + lr;
         const int q = 1 - s;
-        float extra;
-        if (SHFL) {
-            // one shuffle per row: the direction is uniform across the warp
-            extra = q ? __shfl_up_sync(0xffffffffu, mid.w, 1) : __shfl_down_sync(0xffffffffu, mid.x, 1);
-            if (q ? lane == 0 : lane == 31) extra = lds1(oth + ro + (q ? -4 : 16));
-        } else {
-            extra = lds1(oth + ro + (q ? -4 : 16));
-        }
+        const float extra = lds1(oth + ro + (q ? -4 : 16));
         if (y >= 0 && y < H) {
             const float4 v = lds4(own + ro);
             const float4 rh = lds4(rhs + ro);
@@ -248,6 +239,110 @@ __device__ __forceinline__ void tb_relax_block(float *own_p, const float *oth_p,
         }
         up = mid;
         mid = dn;
+    }
+}
+
+// Widths that are a multiple of 8 (KHp = W / 2, no padding slots): the quad
+// of cells x0, x0+2, x0+4, x0+6 with x0 = 2k + 1 - Q.  A cell without some
+// neighbour (x = 0 in the first quad of a Q = 1 row, x = W-1 in the last quad
+// of a Q = 0 row, every cell of the grid's first / last row) takes its own
+// value in that neighbour's place, so the four-term sum minus 4v is the
+// Neumann sum minus cnt v, and is scaled by omega / cnt (we for the edge
+// slot, wa for the others).  Interior cells get exactly the interior form.
+template <int Q>
+__device__ __forceinline__ float4 quad_ghost(float4 v, const float4 &rh, const float4 &u, const float4 &d,
+                                            const float4 &m, float ex, float wa, float we)
+{
+    const float l0 = Q ? ex : m.x, r0v = Q ? m.x : m.y;
+    const float l1 = Q ? m.x : m.y, r1v = Q ? m.y : m.z;
+    const float l2 = Q ? m.y : m.z, r2v = Q ? m.z : m.w;
+    const float l3 = Q ? m.z : m.w, r3v = Q ? m.w : ex;
+    v.x = fmaf(Q ? we : wa, fmaf(-4.f, v.x, (l0 + r0v) + (u.x + d.x)) - rh.x, v.x);
+    v.y = fmaf(wa, fmaf(-4.f, v.y, (l1 + r1v) + (u.y + d.y)) - rh.y, v.y);
+    v.z = fmaf(wa, fmaf(-4.f, v.z, (l2 + r2v) + (u.z + d.z)) - rh.z, v.z);
+    v.w = fmaf(Q ? wa : we, fmaf(-4.f, v.w, (l3 + r3v) + (u.w + d.w)) - rh.w, v.w);
+    return v;
+}
+
+struct QuadIn {
+    float4 v, rh;
+    float ex;
+};
+
+// Loads of one row: the own quad, its r32 and the neighbour one slot beyond
+// the quad (slot k-1 for Q = 1, k+4 for Q = 0; at the row ends these fall in
+// the previous / next plane row and are replaced by the ghost).
+template <int Q>
+__device__ __forceinline__ QuadIn quad_load(unsigned own, unsigned oth, unsigned rhs, unsigned ro)
+{
+    QuadIn in;
+    in.ex = lds1(Q ? oth + ro - 4u : oth + ro + 16u);
+    in.v = lds4(own + ro);
+    in.rh = lds4(rhs + ro);
+    return in;
+}
+
+template <int Q>
+__device__ __forceinline__ void quad_store(unsigned own, unsigned ro, QuadIn in, const float4 &up, const float4 &mid,
+                                           const float4 &dn, int y, int H, bool edge, float we4, const Grid &G)
+{
+    if (y < 0 || y >= H) return;  // halo rows beyond the grid
+    if (edge) in.ex = Q ? in.v.x : in.v.w;
+    float4 nv;
+    if (y > 0 && y < H - 1) {
+        nv = quad_ghost<Q>(in.v, in.rh, up, dn, mid, in.ex, G.w4, we4);
+    } else {
+        const bool two = H > 1;  // vertical neighbours: one, or none when H = 1
+        const float wa = two ? G.w3 : G.w2, we = edge ? (two ? G.w2 : G.w1) : wa;
+        nv = quad_ghost<Q>(in.v, in.rh, y > 0 ? up : in.v, y < H - 1 ? dn : in.v, mid, in.ex, wa, we);
+    }
+    sts4(own + ro, nv);
+}
+
+// tb_relax_block for widths that are a multiple of 8: rows in pairs (a
+// Q = 1 row then a Q = 0 row, parity known at compile time), both rows'
+// loads issued before either store.
+__device__ __forceinline__ void tb_relax_fast(float *own_p, const float *oth_p, const float *rhs_p, int c, int lo,
+                                              int hi, int rb0, int rb1, int ybase, const Grid &G, int KHp, int k)
+{
+    const int H = G.H;
+    int lr = max(lo, rb0);
+    const int l1 = min(hi, rb1);
+    if (lr >= l1) return;
+    const unsigned rb = 4u * (unsigned)KHp;
+    const unsigned own = (unsigned)__cvta_generic_to_shared(own_p) + 4u * k;
+    const unsigned oth = (unsigned)__cvta_generic_to_shared(oth_p) + 4u * k;
+    const unsigned rhs = (unsigned)__cvta_generic_to_shared(rhs_p) + 4u * k;
+    const bool eL = k == 0, eR = k == KHp - 4;
+    const float wL = eL ? G.w3 : G.w4, wR = eR ? G.w3 : G.w4;
+    float4 up = lds4(oth + (unsigned)(lr - 1) * rb), mid = lds4(oth + (unsigned)lr * rb);
+    // Q = 1 - ((y & 1) ^ c)
+    if (((ybase + lr) & 1) ^ c) {
+        const unsigned ro = (unsigned)lr * rb;
+        const float4 dn = lds4(oth + ro + rb);
+        const QuadIn a = quad_load<0>(own, oth, rhs, ro);
+        quad_store<0>(own, ro, a, up, mid, dn, ybase + lr, H, eR, wR, G);
+        up = mid;
+        mid = dn;
+        lr++;
+    }
+#pragma unroll 1
+    for (; lr + 1 < l1; lr += 2) {
+        const unsigned ro = (unsigned)lr * rb;
+        const float4 dn = lds4(oth + ro + rb);
+        const float4 dn2 = lds4(oth + ro + 2 * rb);
+        const QuadIn a = quad_load<1>(own, oth, rhs, ro);
+        const QuadIn b = quad_load<0>(own, oth, rhs, ro + rb);
+        quad_store<1>(own, ro, a, up, mid, dn, ybase + lr, H, eL, wL, G);
+        quad_store<0>(own, ro + rb, b, mid, dn, dn2, ybase + lr + 1, H, eR, wR, G);
+        up = dn;
+        mid = dn2;
+    }
+    if (lr < l1) {
+        const unsigned ro = (unsigned)lr * rb;
+        const float4 dn = lds4(oth + ro + rb);
+        const QuadIn a = quad_load<1>(own, oth, rhs, ro);
+        quad_store<1>(own, ro, a, up, mid, dn, ybase + lr, H, eL, wL, G);
     }
 }
 
@@ -305,7 +400,7 @@ __global__ void __launch_bounds__(kClusterThreads, 1) k_sor_cluster_tb(ClusterAr
     // within one row group when a row group is a whole number of warps
     const int span = n + 2 * HK - 2, L = (span + RP - 1) / RP;
     const int rb0 = rg < RP ? 1 + rg * L : 0, rb1 = rg < RP ? min(rb0 + L, n + 2 * HK - 1) : 0;
-    const bool shfl = (KH4 & 31) == 0;
+    const bool fast = (W & 7) == 0;  // KHp = W / 2: the ghost-cell row form
     __syncthreads();
 
     int sweeps = 0, par = 0, next_check = a.check_every;
@@ -314,15 +409,14 @@ __global__ void __launch_bounds__(kClusterThreads, 1) k_sor_cluster_tb(ClusterAr
         const int kr = min(K, min(a.cycle_cap - sweeps, a.max_iter - done_before - sweeps));
         for (int t = 0; t < kr; t++) {
             const int d = 2 * (kr - t) - 1;
-            if (shfl) {
-                tb_relax_block<true>(P.e[0], P.e[1], P.r[0], 0, HK - d, HK + n + d, rb0, rb1, ybase, G, KHp, k);
+            if (fast) {
+                tb_relax_fast(P.e[0], P.e[1], P.r[0], 0, HK - d, HK + n + d, rb0, rb1, ybase, G, KHp, k);
                 __syncthreads();
-                tb_relax_block<true>(P.e[1], P.e[0], P.r[1], 1, HK - d + 1, HK + n + d - 1, rb0, rb1, ybase, G, KHp, k);
+                tb_relax_fast(P.e[1], P.e[0], P.r[1], 1, HK - d + 1, HK + n + d - 1, rb0, rb1, ybase, G, KHp, k);
             } else {
-                tb_relax_block<false>(P.e[0], P.e[1], P.r[0], 0, HK - d, HK + n + d, rb0, rb1, ybase, G, KHp, k);
+                tb_relax_block(P.e[0], P.e[1], P.r[0], 0, HK - d, HK + n + d, rb0, rb1, ybase, G, KHp, k);
                 __syncthreads();
-                tb_relax_block<false>(P.e[1], P.e[0], P.r[1], 1, HK - d + 1, HK + n + d - 1, rb0, rb1, ybase, G, KHp,
-                                      k);
+                tb_relax_block(P.e[1], P.e[0], P.r[1], 1, HK - d + 1, HK + n + d - 1, rb0, rb1, ybase, G, KHp, k);
             }
             __syncthreads();
         }
@@ -376,14 +470,82 @@ __global__ void __launch_bounds__(kClusterThreads, 1) k_sor_cluster_tb(ClusterAr
     cl.sync();
 }
 
+#include "sor_cluster_rr.cuh"
+
 }  // namespace
 
-int cluster_plan(int dev, int W, int H, int max_depth, int *C_out, size_t *smem_out, int *khp_out, int *depth_out)
+namespace {
+
+bool cluster_fits(const void *fn, int C, int threads, size_t smem)
+{
+    if (cudaFuncSetAttribute(fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess ||
+        cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(C);
+    cfg.blockDim = dim3(threads);
+    cfg.dynamicSmemBytes = smem;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = C;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    int nclusters = 0;
+    if (cudaOccupancyMaxActiveClusters(&nclusters, fn, &cfg) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return nclusters >= 1;
+}
+
+// Register-resident form: W a multiple of 8 up to 512, the band at least HK
+// rows, L = ceil((nmax + 2 HK) / 16) rows per warp in 2..4.
+bool rr_plan(int W, int H, int max_depth, int max_smem, ClusterPlan &p)
+{
+    if (W % 8 != 0 || W > 512 || max_depth < 2) return false;
+    const int KQ = W / 8, NQ = KQ <= 32 ? 1 : 2;
+    for (int C : {16, 8}) {
+        if (H < 2 * C) continue;
+        const int nmax = (H + C - 1) / C, nmin = H / C;
+        for (int K : {4, 2}) {
+            if (K > max_depth) continue;
+            const int HK = 2 * K, R = nmax + 2 * HK;
+            if (nmin < HK) continue;
+            const int L = std::max(2, (R + kRRWarps - 1) / kRRWarps);
+            const void *fn = rr_kernel(K, L, NQ);
+            if (!fn) continue;
+            const size_t smem = rr_floats(K, NQ, R) * sizeof(float);
+            if (smem + 2048 > (size_t)max_smem) continue;
+            if (!cluster_fits(fn, C, kRRThreads, smem)) continue;
+            p.C = C;
+            p.smem = smem;
+            p.khp = ((W + 1) / 2 + 3) / 4 * 4;
+            p.depth = K;
+            p.rr_l = L;
+            p.rr_nq = NQ;
+            return true;
+        }
+    }
+    return false;
+}
+
+}  // namespace
+
+int cluster_plan(int dev, int W, int H, int max_depth, ClusterPlan *plan)
 {
     int max_smem = 0, cluster_ok = 0;
     PCD_CUDA(cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
     PCD_CUDA(cudaDeviceGetAttribute(&cluster_ok, cudaDevAttrClusterLaunch, dev));
     if (!cluster_ok) return PCD_BAD_ARG;
+    ClusterPlan p{};
+    if (rr_plan(W, H, max_depth, max_smem, p)) {
+        *plan = p;
+        return PCD_OK;
+    }
     const int khp = ((W + 1) / 2 + 3) / 4 * 4;
     if (khp / 2 > kClusterThreads) return PCD_BAD_ARG;
     for (int C : {16, 8}) {
@@ -402,52 +564,47 @@ int cluster_plan(int dev, int W, int H, int max_depth, int *C_out, size_t *smem_
                 fn = depth == 2 ? (const void *)k_sor_cluster_tb<2> : (const void *)k_sor_cluster_tb<1>;
             }
             if (smem + 2048 > (size_t)max_smem) continue;
-            PCD_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
-            PCD_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-            cudaLaunchConfig_t cfg = {};
-            cfg.gridDim = dim3(C);
-            cfg.blockDim = dim3(kClusterThreads);
-            cfg.dynamicSmemBytes = smem;
-            cudaLaunchAttribute attr[1];
-            attr[0].id = cudaLaunchAttributeClusterDimension;
-            attr[0].val.clusterDim.x = C;
-            attr[0].val.clusterDim.y = 1;
-            attr[0].val.clusterDim.z = 1;
-            cfg.attrs = attr;
-            cfg.numAttrs = 1;
-            int nclusters = 0;
-            if (cudaOccupancyMaxActiveClusters(&nclusters, fn, &cfg) != cudaSuccess) {
-                cudaGetLastError();
-                continue;
-            }
-            if (nclusters < 1) continue;
-            *C_out = C;
-            *smem_out = smem;
-            *khp_out = khp;
-            *depth_out = depth;
+            if (!cluster_fits(fn, C, kClusterThreads, smem)) continue;
+            p.C = C;
+            p.smem = smem;
+            p.khp = khp;
+            p.depth = depth;
+            *plan = p;
             return PCD_OK;
         }
     }
     return PCD_BAD_ARG;
 }
 
-int launch_cluster(ClusterArgs &a, int C, size_t smem, cudaStream_t s)
+int launch_cluster(ClusterArgs &a, const ClusterPlan &p, cudaStream_t s)
 {
     cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(C);
-    cfg.blockDim = dim3(kClusterThreads);
-    cfg.dynamicSmemBytes = smem;
+    cfg.gridDim = dim3(p.C);
+    cfg.blockDim = dim3(p.rr_l ? kRRThreads : kClusterThreads);
+    cfg.dynamicSmemBytes = p.smem;
     cfg.stream = s;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeClusterDimension;
-    attr[0].val.clusterDim.x = C;
+    attr[0].val.clusterDim.x = p.C;
     attr[0].val.clusterDim.y = 1;
     attr[0].val.clusterDim.z = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    if (a.depth == 2) PCD_CUDA(cudaLaunchKernelEx(&cfg, k_sor_cluster_tb<2>, a));
-    else if (a.depth == 1) PCD_CUDA(cudaLaunchKernelEx(&cfg, k_sor_cluster_tb<1>, a));
-    else PCD_CUDA(cudaLaunchKernelEx(&cfg, k_sor_cluster, a));
+    a.depth = p.depth;
+    if (p.rr_l) {
+        const void *fn = rr_kernel(p.depth, p.rr_l, p.rr_nq);
+        if (!fn) {
+            set_error("cluster SOR: no register-resident kernel for this plan");
+            return PCD_BAD_ARG;
+        }
+        PCD_CUDA(cudaLaunchKernelEx(&cfg, reinterpret_cast<void (*)(ClusterArgs)>(const_cast<void *>(fn)), a));
+    } else if (p.depth == 2) {
+        PCD_CUDA(cudaLaunchKernelEx(&cfg, k_sor_cluster_tb<2>, a));
+    } else if (p.depth == 1) {
+        PCD_CUDA(cudaLaunchKernelEx(&cfg, k_sor_cluster_tb<1>, a));
+    } else {
+        PCD_CUDA(cudaLaunchKernelEx(&cfg, k_sor_cluster, a));
+    }
     count_launches(1);
     return PCD_OK;
 }

@@ -20,14 +20,26 @@ struct ClusterArgs {
     double drop;         // end the cycle when the estimate fell by this factor
     float w32[5];        // omega / cnt
     float one_minus_omega;
-    int depth;           // sweeps between halo exchanges (1 or 2; 0: one exchange per half sweep)
+    int depth;           // sweeps between halo exchanges (1, 2 or 4; 0: one exchange per half sweep)
 };
 
-// Cluster size (16 or 8 CTAs), sweeps per halo exchange and dynamic shared
-// memory for a W x H grid; PCD_BAD_ARG when the grid does not fit in one
+// How one grid runs on one cluster: C CTAs (16 or 8), dynamic shared memory,
+// the shared-memory plane stride, the sweeps per halo exchange (0: one
+// exchange per half sweep) and, for the register-resident form, the rows per
+// warp and quads per lane (rr_l = 0: the shared-memory forms).
+struct ClusterPlan {
+    int C;
+    size_t smem;
+    int khp;
+    int depth;
+    int rr_l;
+    int rr_nq;
+};
+
+// The plan for a W x H grid; PCD_BAD_ARG when the grid does not fit in one
 // cluster.  max_depth caps the sweeps per exchange (0: the per-half-sweep
-// exchange).
-int cluster_plan(int dev, int W, int H, int max_depth, int *C_out, size_t *smem_out, int *khp_out, int *depth_out);
-int launch_cluster(ClusterArgs &a, int C, size_t smem, cudaStream_t s);
+// exchange; the register-resident form needs at least 2).
+int cluster_plan(int dev, int W, int H, int max_depth, ClusterPlan *plan);
+int launch_cluster(ClusterArgs &a, const ClusterPlan &p, cudaStream_t s);
 
 }  // namespace pcd

@@ -126,14 +126,17 @@ def test_stream_sweeps_match_launch_schedule(ctx, n, m, ld):
     assert err < 1e-5, err
 
 
-@pytest.mark.parametrize("n,m", [(512, 512), (96, 80), (640, 480), (33, 17), (1024, 300), (1024, 400)])
+@pytest.mark.parametrize("n,m", [(512, 512), (96, 80), (640, 480), (33, 17), (1024, 300), (1024, 400), (256, 256),
+                                 (384, 200), (504, 700), (136, 64), (512, 33)])
 def test_cluster_sweeps_match_launch_schedule(ctx, n, m):
-    """The cluster schedule (FP32 sweeps in distributed shared memory, two or
-    one sweeps per halo exchange with the halo rows recomputed, or one
-    exchange per half sweep when the halo does not fit: 1024 x 400) runs the
-    same red-black iteration as the launch-per-half-sweep kernels: after the
-    same odd number of mixed-precision sweeps (a last round of one sweep) the
-    iterates agree to FP32 rounding."""
+    """The cluster schedule runs the same red-black iteration as the
+    launch-per-half-sweep kernels: after the same odd number of mixed-precision
+    sweeps (a last round shorter than the others) the iterates agree to FP32
+    rounding.  Widths that are a multiple of 8 up to 512 take the
+    register-resident form (4 or 2 sweeps per exchange, 1 or 2 quads per
+    lane, 2 to 4 rows per warp, idle lanes at 384 and 136 columns); the others
+    the shared-memory forms (two or one sweeps per halo exchange, or one
+    exchange per half sweep when the halo does not fit: 1024 x 400)."""
     import poisson_caustic_design_gb300 as pcd
 
     b = pcd.inputs.poisson_rhs(n, 4, "gaussian", m=m)
