@@ -10,8 +10,8 @@
 // from the warp's own registers except across warp boundaries, where each
 // warp publishes its first and last row of the colour it just relaxed in
 // shared memory (double-buffered by colour, so one block barrier per half
-// sweep).  The right-hand side r32 stays in shared memory (one 16-byte load
-// per quad and half sweep).
+// sweep).  The right-hand side stays in shared memory, negated (one 16-byte
+// load per quad and half sweep); the update runs in packed FP32 pairs.
 //
 // Temporal blocking as in k_sor_cluster_tb: K sweeps per halo exchange on the
 // band and HK = 2K halo rows on each side, the halo recomputed with the same
@@ -40,33 +40,40 @@ __host__ __device__ inline size_t rr_floats(int K, int NQ, int R)
 }
 
 // The update of quad_ghost with the parity q as an argument (folded to a
-// constant where the caller's q is one).
-__device__ __forceinline__ float4 quad_ghost_q(int q, float4 v, const float4 &rh, const float4 &u, const float4 &d,
-                                              const float4 &m, float ex, float wa, float we)
+// constant where the caller's q is one), in packed FP32 pairs: cells (x, y)
+// and (z, w) of the quad share one instruction per step.  nrh is -r32.  The
+// steps and their rounding are those of the scalar form
+// v + w ((l + r) + (u + d) - 4 v - r32).
+__device__ __forceinline__ float4 quad_ghost_q(int q, const float4 &v, const float4 &nrh, const float4 &u,
+                                              const float4 &d, const float4 &m, float ex, float2 wA, float2 wB)
 {
-    const float l0 = q ? ex : m.x, r0v = q ? m.x : m.y;
-    const float l1 = q ? m.x : m.y, r1v = q ? m.y : m.z;
-    const float l2 = q ? m.y : m.z, r2v = q ? m.z : m.w;
-    const float l3 = q ? m.z : m.w, r3v = q ? m.w : ex;
-    v.x = fmaf(q ? we : wa, fmaf(-4.f, v.x, (l0 + r0v) + (u.x + d.x)) - rh.x, v.x);
-    v.y = fmaf(wa, fmaf(-4.f, v.y, (l1 + r1v) + (u.y + d.y)) - rh.y, v.y);
-    v.z = fmaf(wa, fmaf(-4.f, v.z, (l2 + r2v) + (u.z + d.z)) - rh.z, v.z);
-    v.w = fmaf(q ? wa : we, fmaf(-4.f, v.w, (l3 + r3v) + (u.w + d.w)) - rh.w, v.w);
-    return v;
+    const float h0 = q ? ex + m.x : m.x + m.y;
+    const float h1 = q ? m.x + m.y : m.y + m.z;
+    const float h2 = q ? m.y + m.z : m.z + m.w;
+    const float h3 = q ? m.z + m.w : m.w + ex;
+    const float2 vA = make_float2(v.x, v.y), vB = make_float2(v.z, v.w);
+    const float2 m4 = make_float2(-4.f, -4.f);
+    float2 tA = __fadd2_rn(make_float2(h0, h1), __fadd2_rn(make_float2(u.x, u.y), make_float2(d.x, d.y)));
+    float2 tB = __fadd2_rn(make_float2(h2, h3), __fadd2_rn(make_float2(u.z, u.w), make_float2(d.z, d.w)));
+    tA = __fadd2_rn(__ffma2_rn(m4, vA, tA), make_float2(nrh.x, nrh.y));
+    tB = __fadd2_rn(__ffma2_rn(m4, vB, tB), make_float2(nrh.z, nrh.w));
+    const float2 nA = __ffma2_rn(wA, tA, vA), nB = __ffma2_rn(wB, tB, vB);
+    return make_float4(nA.x, nA.y, nB.x, nB.y);
 }
 
-// Sum of squares of r - L v over the quad (ghost neighbours as above).
-__device__ __forceinline__ float quad_ghost_res2(int q, const float4 &v, const float4 &rh, const float4 &u,
+// Sum of squares of r32 - L v over the quad (ghost neighbours as above; nrh
+// is -r32).
+__device__ __forceinline__ float quad_ghost_res2(int q, const float4 &v, const float4 &nrh, const float4 &u,
                                                 const float4 &d, const float4 &m, float ex)
 {
     const float l0 = q ? ex : m.x, r0v = q ? m.x : m.y;
     const float l1 = q ? m.x : m.y, r1v = q ? m.y : m.z;
     const float l2 = q ? m.y : m.z, r2v = q ? m.z : m.w;
     const float l3 = q ? m.z : m.w, r3v = q ? m.w : ex;
-    const float a0 = rh.x - fmaf(-4.f, v.x, (l0 + r0v) + (u.x + d.x));
-    const float a1 = rh.y - fmaf(-4.f, v.y, (l1 + r1v) + (u.y + d.y));
-    const float a2 = rh.z - fmaf(-4.f, v.z, (l2 + r2v) + (u.z + d.z));
-    const float a3 = rh.w - fmaf(-4.f, v.w, (l3 + r3v) + (u.w + d.w));
+    const float a0 = nrh.x + fmaf(-4.f, v.x, (l0 + r0v) + (u.x + d.x));
+    const float a1 = nrh.y + fmaf(-4.f, v.y, (l1 + r1v) + (u.y + d.y));
+    const float a2 = nrh.z + fmaf(-4.f, v.z, (l2 + r2v) + (u.z + d.z));
+    const float a3 = nrh.w + fmaf(-4.f, v.w, (l3 + r3v) + (u.w + d.w));
     return fmaf(a0, a0, fmaf(a1, a1, fmaf(a2, a2, a3 * a3)));
 }
 
@@ -74,11 +81,11 @@ template <int K, int L, int NQ>
 struct RRState {
     static constexpr int HK = 2 * K, KS = 128 * NQ;
     float4 e[2][L][NQ];      // both colours of the warp's rows
-    float wa[NQ], wl[NQ], wr[NQ];
+    float2 waa[NQ], wla[NQ], war[NQ];  // weight pairs: (wa, wa), (wl, wa), (wa, wr)
     bool act[NQ], eL[NQ], eR[NQ];
-    float w3, w2, w1;
+    float w4, w3, w2, w1;
     int lane, w, H, ybase, R;
-    unsigned edge_s, r_s;    // shared addresses of slot 4 * lane of edge row 0 / r32 row 0
+    unsigned edge_s, r_s;    // shared addresses of slot 4 * lane of edge row 0 / -r32 row 0
 
     __device__ __forceinline__ unsigned edge_addr(int c, int ww, int side) const
     {
@@ -133,11 +140,14 @@ struct RRState {
             // no row of the warp in range
         } else if (y0 > 0 && y0 + L < H) {
             // every row of the warp is an interior grid row: no branches, so
-            // the quads of all rows interleave; rows outside [lo, hi) take
-            // weight 0 and keep their values
+            // the quads of all rows interleave.  Rows of the warp outside
+            // [lo, hi) are relaxed too: they lie in the halo outside the
+            // dependency cone of the band (a row in [lo, hi) reads only rows
+            // of the previous half sweep's range), and the halo is
+            // overwritten at the next exchange; rows past the CTA's plane
+            // stay bounded and are never read by a band row.
 #pragma unroll
             for (int j = 0; j < L; j++) {
-                const bool on = lr0 + j >= lo && lr0 + j < hi;
                 const int q = 1 - ((P ^ j ^ CC) & 1);
                 // rows past the plane (16 L > R) read its last row, and are dropped
                 const unsigned rrow = r_s + 4u * (unsigned)((CC * R + min(lr0 + j, R - 1)) * KS);
@@ -149,18 +159,22 @@ struct RRState {
                     if (q ? eL[i] : eR[i]) ex = q ? v.x : v.w;
                     const float4 u = j > 0 ? e[OC][j > 0 ? j - 1 : 0][i] : eu[i];
                     const float4 d = j + 1 < L ? e[OC][j + 1 < L ? j + 1 : j][i] : ed[i];
-                    const float wA = on ? wa[i] : 0.f, wE = on ? (q ? wl[i] : wr[i]) : 0.f;
-                    e[CC][j][i] = quad_ghost_q(q, v, rh, u, d, e[OC][j][i], ex, wA, wE);
+                    e[CC][j][i] = quad_ghost_q(q, v, rh, u, d, e[OC][j][i], ex, q ? wla[i] : waa[i], q ? waa[i] : war[i]);
                 }
             }
         } else {
+            // a warp holding the grid's first or last row (or rows beyond
+            // it): branch free as well, rows outside the grid with weight 0,
+            // the first / last row with its missing neighbour's ghost and
+            // weight omega / (cnt)
+            const bool two = H > 1;
 #pragma unroll
             for (int j = 0; j < L; j++) {
                 const int lr = lr0 + j, y = ybase + lr;
-                if (lr < lo || lr >= hi || y < 0 || y >= H) continue;  // uniform over the warp
+                const bool on = lr >= lo && lr < hi && y >= 0 && y < H;
+                const bool top = y == 0, bot = y == H - 1, brd = top || bot;
                 const int q = 1 - ((P ^ j ^ CC) & 1);
-                const bool inner = y > 0 && y < H - 1;
-                const unsigned rrow = r_s + 4u * (unsigned)((CC * R + lr) * KS);
+                const unsigned rrow = r_s + 4u * (unsigned)((CC * R + min(lr, R - 1)) * KS);
 #pragma unroll
                 for (int i = 0; i < NQ; i++) {
                     const float4 v = e[CC][j][i];
@@ -170,18 +184,12 @@ struct RRState {
                     if (edge) ex = q ? v.x : v.w;
                     float4 u = j > 0 ? e[OC][j > 0 ? j - 1 : 0][i] : eu[i];
                     float4 d = j + 1 < L ? e[OC][j + 1 < L ? j + 1 : j][i] : ed[i];
-                    float wA, wE;
-                    if (inner) {
-                        wA = wa[i];
-                        wE = q ? wl[i] : wr[i];
-                    } else {
-                        if (y == 0) u = v;
-                        if (y == H - 1) d = v;
-                        const bool two = H > 1;
-                        wA = act[i] ? (two ? w3 : w2) : 0.f;
-                        wE = edge ? (two ? w2 : w1) : wA;
-                    }
-                    e[CC][j][i] = quad_ghost_q(q, v, rh, u, d, e[OC][j][i], ex, wA, wE);
+                    if (top) u = v;
+                    if (bot) d = v;
+                    const float a = !on || !act[i] ? 0.f : brd ? (two ? w3 : w2) : w4;
+                    const float we = !on ? 0.f : edge ? (brd ? (two ? w2 : w1) : w3) : a;
+                    const float2 wA = make_float2(q ? we : a, a), wB = make_float2(a, q ? a : we);
+                    e[CC][j][i] = quad_ghost_q(q, v, rh, u, d, e[OC][j][i], ex, wA, wB);
                 }
             }
         }
@@ -261,6 +269,7 @@ __global__ void __launch_bounds__(kRRThreads, 1) k_sor_cluster_rr(ClusterArgs a)
     st.R = R;
     st.edge_s = (unsigned)__cvta_generic_to_shared(edge) + 16u * lane;
     st.r_s = (unsigned)__cvta_generic_to_shared(rp) + 16u * lane;
+    st.w4 = a.w32[4];
     st.w3 = a.w32[3];
     st.w2 = a.w32[2];
     st.w1 = a.w32[1];
@@ -271,9 +280,10 @@ __global__ void __launch_bounds__(kRRThreads, 1) k_sor_cluster_rr(ClusterArgs a)
         st.act[i] = qi < KQ;
         st.eL[i] = qi == 0;
         st.eR[i] = qi == KQ - 1;
-        st.wa[i] = st.act[i] ? a.w32[4] : 0.f;
-        st.wl[i] = st.eL[i] ? a.w32[3] : st.wa[i];
-        st.wr[i] = st.eR[i] ? a.w32[3] : st.wa[i];
+        const float wa = st.act[i] ? a.w32[4] : 0.f;
+        st.waa[i] = make_float2(wa, wa);
+        st.wla[i] = make_float2(st.eL[i] ? a.w32[3] : wa, wa);
+        st.war[i] = make_float2(wa, st.eR[i] ? a.w32[3] : wa);
     }
     // own and halo rows of e (registers) and r32 (shared) from global memory
     const int Rn = n + 2 * HK;
@@ -291,7 +301,7 @@ __global__ void __launch_bounds__(kRRThreads, 1) k_sor_cluster_rr(ClusterArgs a)
                 if (in && qi < KQ) {
                     const size_t b0 = (size_t)y * a.ld + 8 * qi + sc;
                     ev = make_float4(a.e[b0], a.e[b0 + 2], a.e[b0 + 4], a.e[b0 + 6]);
-                    rv = make_float4(a.r32[b0], a.r32[b0 + 2], a.r32[b0 + 4], a.r32[b0 + 6]);
+                    rv = make_float4(-a.r32[b0], -a.r32[b0 + 2], -a.r32[b0 + 4], -a.r32[b0 + 6]);
                 }
                 st.e[c][j][i] = ev;
                 if (lr < R) reinterpret_cast<float4 *>(rp + (size_t)(c * R + lr) * KS)[qi] = rv;
