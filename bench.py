@@ -375,7 +375,7 @@ def run_ours(args, rank, world, local, pg):
         print("e2e samples (ms): " + " ".join(f"{t:.2f}" for t in e2e_ms), file=sys.stderr, flush=True)
 
     # roofline of the dominant kernel of the headline step: the FP32 cluster
-    # sweep kernel (k_sor_cluster_tb).  Algorithmic bytes per cell-sweep: 12
+    # sweep kernel (k_sor_cluster_rr).  Algorithmic bytes per cell-sweep: 12
     # (read e, read r32, write e in FP32), over the sweep kernels' device time
     # (CUDA events on the context stream around the cycle loop).
     hm = results[headline]
@@ -385,10 +385,10 @@ def run_ours(args, rank, world, local, pg):
     peak, peak_src = measured_hbm_peak()
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
             "traffic": None, "peak_source": peak_src,
-            "kernel": "k_sor_cluster_tb (FP32 sweeps)", "alg_bytes_per_solve": alg_bytes,
-            "note": "the 512^2 working set stays in the cluster's shared memory for a whole FP32 cycle: "
-                    "the kernel is bound by shared-memory issue and cluster barriers, not HBM; DRAM traffic "
-                    "per launch is the band load and store (ncu summary under profiles/)"}
+            "kernel": "k_sor_cluster_rr (FP32 sweeps)", "alg_bytes_per_solve": alg_bytes,
+            "note": "the 512^2 working set stays on one 16-CTA cluster for a whole FP32 cycle (e in registers, "
+                    "r32 in shared memory): the kernel is bound by FP32 issue, block and cluster barriers, not "
+                    "HBM; DRAM traffic per launch is the band load and store (ncu summary under profiles/)"}
 
     # batched configuration: 64 instances, sizes uniform in {64..1024}^2, one
     # persistent cluster launch (CUDA graph); FP32 sweeps, FP64 residuals

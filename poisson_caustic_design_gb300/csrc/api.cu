@@ -27,6 +27,112 @@ std::atomic<unsigned long long> g_launches{0};
 void set_error(const std::string &msg) { g_last_error = msg; }
 void count_launches(unsigned long long n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 
+namespace {
+
+// Keeps the smoothed prediction when its residual is below the smoothed zero
+// guess's (a NaN residual never is), else a zero start; records the verdict.
+__global__ void k_judge_pick(const Ctl *cz, const Ctl *cp, const double *__restrict__ pred, double *__restrict__ phi,
+                             int W, int H, int ld, JudgeOut *out)
+{
+    const double rz = cz->rel, rp = cp->rel;
+    const bool keep = rp < rz;
+    const long n = (long)W * H;
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+        const long y = i / W, j = y * ld + (i - y * W);
+        phi[j] = keep ? pred[j] : 0.0;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        out->keep = keep ? 1 : 0;
+        out->rel_pred = rp;
+        out->rel_zero = rz;
+    }
+}
+
+// (Re)builds the judge graph for this shape and network: buffers sized for
+// H * ld cells, then the prediction, the zero guess and both smoothings
+// captured from the context's stream.
+int judge_prepare(pcd_ctx *ctx, int W, int H, int ld, cudaStream_t s)
+{
+    JudgeGraph &J = ctx->judge;
+    UNet &net = ctx->net->net;
+    if (J.exec && J.W == W && J.H == H && J.ld == ld && J.net == (const void *)ctx->net && J.arena == net.arena)
+        return PCD_OK;
+    if (J.exec) {
+        cudaGraphExecDestroy(J.exec);
+        J.exec = nullptr;
+    }
+    const size_t cells = (size_t)H * ld;
+    if (cells > J.cells) {
+        PCD_CUDA(cudaStreamSynchronize(s));
+        if (J.b) cudaFree(J.b);
+        if (J.pred) cudaFree(J.pred);
+        if (J.zero) cudaFree(J.zero);
+        if (J.mask) cudaFree(J.mask);
+        J.b = J.pred = J.zero = nullptr;
+        J.mask = nullptr;
+        J.cells = 0;
+        PCD_CUDA(cudaMalloc(&J.b, cells * sizeof(double)));
+        PCD_CUDA(cudaMalloc(&J.pred, cells * sizeof(double)));
+        PCD_CUDA(cudaMalloc(&J.zero, cells * sizeof(double)));
+        PCD_CUDA(cudaMalloc(&J.mask, cells));
+        J.cells = cells;
+    }
+    if (!J.ctl) {
+        PCD_CUDA(cudaMalloc(&J.ctl, 2 * sizeof(Ctl)));
+        PCD_CUDA(cudaMalloc(&J.partials, residual_partials_bytes()));
+        PCD_CUDA(cudaMalloc(&J.out, sizeof(JudgeOut)));
+        PCD_CUDA(cudaMallocHost(&J.out_host, sizeof(JudgeOut)));
+        PCD_CUDA(cudaEventCreateWithFlags(&J.done, cudaEventDisableTiming));
+    }
+    const unsigned long long n0 = g_launches.load();
+    cudaGraph_t g;
+    PCD_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    int st = net.warm_start(J.b, W, H, ld, J.pred, s);
+    if (st == PCD_OK) st = zero_grid(J.zero, W, H, ld, s);
+    if (st == PCD_OK) st = enqueue_smooth(J.b, J.zero, J.mask, J.ctl, J.partials, W, H, ld, kLearnedSmooth, 1.0, s);
+    if (st == PCD_OK)
+        st = enqueue_smooth(J.b, J.pred, J.mask, J.ctl + 1, J.partials, W, H, ld, kLearnedSmooth, 1.0, s);
+    const cudaError_t ce = cudaStreamEndCapture(s, &g);
+    // nothing ran during the capture: count the kernels at each replay instead
+    J.launches = g_launches.load() - n0;
+    g_launches.fetch_sub(J.launches, std::memory_order_relaxed);
+    if (st != PCD_OK) return st;
+    if (ce != cudaSuccess) {
+        set_error(std::string("judge graph capture: ") + cudaGetErrorString(ce));
+        return PCD_DEVICE_ERROR;
+    }
+    const cudaError_t ie = cudaGraphInstantiate(&J.exec, g, 0);
+    cudaGraphDestroy(g);
+    if (ie != cudaSuccess) {
+        J.exec = nullptr;
+        set_error(std::string("judge graph instantiate: ") + cudaGetErrorString(ie));
+        return PCD_DEVICE_ERROR;
+    }
+    J.W = W;
+    J.H = H;
+    J.ld = ld;
+    J.net = ctx->net;
+    J.arena = net.arena;
+    return PCD_OK;
+}
+
+}  // namespace
+
+void JudgeGraph::release()
+{
+    if (exec) cudaGraphExecDestroy(exec);
+    if (b) cudaFree(b);
+    if (pred) cudaFree(pred);
+    if (zero) cudaFree(zero);
+    if (mask) cudaFree(mask);
+    if (ctl) cudaFree(ctl);
+    if (partials) cudaFree(partials);
+    if (out) cudaFree(out);
+    if (out_host) cudaFreeHost(out_host);
+    if (done) cudaEventDestroy(done);
+    *this = JudgeGraph();
+}
+
 int ctx_stage(pcd_ctx *ctx, size_t cells)
 {
     if (cells > ctx->host_cells) {
@@ -65,43 +171,53 @@ int ctx_activate(pcd_ctx *ctx)
 }
 
 // Solve with the warm-start policy of o: the learned prediction is kept only
-// when its FP64 residual is below that of a zero guess (||b||).
+// when its smoothed FP64 residual is below that of a smoothed zero guess.
 int solve_with_warm_start(pcd_ctx *ctx, const double *b, double *phi, int W, int H, int ld, pcd_solve_opts o,
                           pcd_solve_stats *stats, cudaStream_t s)
 {
     int used = o.warm_start == PCD_WARM_GIVEN ? 1 : 0;
     double rel0 = -1.0, relz = -1.0;
     int pre_sweeps = 0;
+    bool judged = false;
     if (o.warm_start == PCD_WARM_LEARNED) {
         if (!ctx->net) {
             set_error("warm_start = PCD_WARM_LEARNED needs a network (pcd_ctx_set_warm_start_net)");
             return PCD_BAD_ARG;
         }
-        PCD_TRY(ctx->net->net.warm_start(b, W, H, ld, phi, s));
         // Judge the prediction after kLearnedSmooth Gauss-Seidel sweeps (red-
         // black, omega = 1) against a zero guess after the same sweeps: the
         // sweeps remove the cell-scale error that the prediction's
         // interpolation and BF16 arithmetic leave (it would dominate the raw
         // residual), and the zero guess's residual also moves under them.
-        // The prediction is kept when its smoothed residual is the smaller.
-        PCD_TRY(ctx->solver.reserve((size_t)H * ld));
-        double *zero_phi = ctx->solver.r64;  // scratch: the solve rewrites it
-        PCD_TRY(zero_grid(zero_phi, W, H, ld, s));
-        PCD_TRY(smooth_residual(ctx->solver, b, zero_phi, W, H, ld, kLearnedSmooth, 1.0, s, &relz));
-        PCD_TRY(smooth_residual(ctx->solver, b, phi, W, H, ld, kLearnedSmooth, 1.0, s, &rel0));
-        if (rel0 < relz) {
-            used = 2;
-            pre_sweeps = kLearnedSmooth;
-        } else {  // not better than a zero guess (or not finite): start from zero
-            PCD_TRY(zero_grid(phi, W, H, ld, s));
-            used = 3;
-        }
+        // The smoothed prediction is kept when its residual is the smaller.
+        // All on the device: b in, one graph replay, the pick, the verdict
+        // read back after the solve.
+        JudgeGraph &J = ctx->judge;
+        PCD_TRY(judge_prepare(ctx, W, H, ld, s));
+        PCD_CUDA(cudaMemcpy2DAsync(J.b, (size_t)ld * sizeof(double), b, (size_t)ld * sizeof(double),
+                                   (size_t)W * sizeof(double), H, cudaMemcpyDeviceToDevice, s));
+        PCD_CUDA(cudaGraphLaunch(J.exec, s));
+        count_launches(J.launches);
+        const int pblocks = (int)std::min<long>(1216, ((long)W * H + 255) / 256);
+        k_judge_pick<<<pblocks, 256, 0, s>>>(J.ctl, J.ctl + 1, J.pred, phi, W, H, ld, J.out);
+        PCD_LAUNCHED(1);
+        PCD_CUDA(cudaMemcpyAsync(J.out_host, J.out, sizeof(JudgeOut), cudaMemcpyDeviceToHost, s));
+        PCD_CUDA(cudaEventRecord(J.done, s));
+        judged = true;
         o.warm_start = PCD_WARM_GIVEN;
     } else if (o.warm_start != PCD_WARM_ZERO && o.warm_start != PCD_WARM_GIVEN) {
         set_error("pcd solve: unknown warm_start");
         return PCD_BAD_ARG;
     }
     int st = solve_autotuned(ctx, b, phi, W, H, ld, o, stats, s);
+    if (judged) {
+        PCD_CUDA(cudaEventSynchronize(ctx->judge.done));
+        const JudgeOut &v = *ctx->judge.out_host;
+        used = v.keep ? 2 : 3;
+        pre_sweeps = v.keep ? kLearnedSmooth : 0;
+        rel0 = v.rel_pred;
+        relz = v.rel_zero;
+    }
     if (stats) {
         stats->warm_used = used;
         stats->warm_rel_residual = rel0;
@@ -195,6 +311,7 @@ int pcd_ctx_destroy(pcd_ctx *ctx)
     ctx->grid.release();
     ctx->batch.release();
     ctx->tuner.release();
+    ctx->judge.release();
     if (ctx->d_b) cudaFree(ctx->d_b);
     if (ctx->d_phi) cudaFree(ctx->d_phi);
     if (ctx->join_in) cudaEventDestroy(ctx->join_in);

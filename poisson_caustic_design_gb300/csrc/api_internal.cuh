@@ -32,6 +32,36 @@ struct Autotuner {
 };
 }  // namespace pcd
 
+namespace pcd {
+// Result of the learned warm start's judge: whether the prediction was kept
+// and the two smoothed relative residuals.
+struct JudgeOut {
+    int keep;
+    int pad_;
+    double rel_pred, rel_zero;
+};
+
+// The learned warm start and its judge (prediction, kLearnedSmooth Gauss-
+// Seidel sweeps on it and on a zero guess, both FP64 residuals) as one CUDA
+// graph per grid shape and network, on buffers of its own: the caller's b is
+// copied in before the replay and the chosen start copied out after it, so a
+// solve with the learned warm start has no host round trip before the solver.
+struct JudgeGraph {
+    int W = 0, H = 0, ld = 0;
+    const void *net = nullptr, *arena = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    unsigned long long launches = 0;  // kernels per replay
+    size_t cells = 0;
+    double *b = nullptr, *pred = nullptr, *zero = nullptr, *partials = nullptr;
+    uint8_t *mask = nullptr;
+    Ctl *ctl = nullptr;             // [2]: zero guess, prediction
+    JudgeOut *out = nullptr;        // device
+    JudgeOut *out_host = nullptr;   // pinned
+    cudaEvent_t done = nullptr;
+    void release();
+};
+}  // namespace pcd
+
 struct pcd_ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
@@ -52,6 +82,7 @@ struct pcd_ctx {
     // networks created on this context; their device state is released with it
     std::set<pcd_unet *> nets;
     pcd::Autotuner tuner;
+    pcd::JudgeGraph judge;
 };
 
 namespace pcd {

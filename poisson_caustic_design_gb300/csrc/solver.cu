@@ -903,10 +903,9 @@ int residual_rel(SolverWorkspace &ws, const double *b, const double *phi, int W,
     return PCD_OK;
 }
 
-int smooth_residual(SolverWorkspace &ws, const double *b, double *phi, int W, int H, int ld, int sweeps, double omega,
-                    cudaStream_t s, double *rel)
+int enqueue_smooth(const double *b, double *phi, uint8_t *mask, Ctl *ctl, double *partials, int W, int H, int ld,
+                   int sweeps, double omega, cudaStream_t s)
 {
-    PCD_TRY(ws.reserve((size_t)H * ld));
     SolveArgs a{};
     a.W = W; a.H = H; a.ld = ld;
     a.stop = PCD_STOP_REL_RESIDUAL;
@@ -917,19 +916,29 @@ int smooth_residual(SolverWorkspace &ws, const double *b, double *phi, int W, in
         a.w64[c] = omega / (double)c;
         a.w32[c] = (float)omega / (float)c;
     }
-    PCD_CUDA(cudaMemsetAsync(ws.ctl, 0, sizeof(Ctl), s));
+    PCD_CUDA(cudaMemsetAsync(ctl, 0, sizeof(Ctl), s));
     const int rblocks = grid_blocks((long)W * H);
-    k_mask<<<rblocks, kThreads, 0, s>>>(b, ws.mask, W, H, ld, ws.ctl);
+    k_mask<<<rblocks, kThreads, 0, s>>>(b, mask, W, H, ld, ctl);
     PCD_LAUNCHED(1);
     const int half = (W + 1) >> 1;
     const int blocks = ceil_div((long)H * half, kThreads);
     for (int k = 0; k < sweeps; k++)
         for (int color = 0; color < 2; color++) {
-            k_rb_half<double, true, false><<<blocks, kThreads, 0, s>>>(phi, b, ws.mask, ws.ctl, a, color, color);
+            k_rb_half<double, true, false><<<blocks, kThreads, 0, s>>>(phi, b, mask, ctl, a, color, color);
             PCD_LAUNCHED(1);
         }
-    k_residual64<true><<<rblocks, kThreads, 0, s>>>(phi, b, ws.mask, ws.ctl, ws.partials, a, 0, 1, 0);
+    k_residual64<true><<<rblocks, kThreads, 0, s>>>(phi, b, mask, ctl, partials, a, 0, 1, 0);
     PCD_LAUNCHED(1);
+    return PCD_OK;
+}
+
+size_t residual_partials_bytes() { return sizeof(double) * 3 * kResidualBlocksMax; }
+
+int smooth_residual(SolverWorkspace &ws, const double *b, double *phi, int W, int H, int ld, int sweeps, double omega,
+                    cudaStream_t s, double *rel)
+{
+    PCD_TRY(ws.reserve((size_t)H * ld));
+    PCD_TRY(enqueue_smooth(b, phi, ws.mask, ws.ctl, ws.partials, W, H, ld, sweeps, omega, s));
     PCD_CUDA(cudaMemcpyAsync(ws.ctl_host, ws.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, s));
     PCD_CUDA(cudaStreamSynchronize(s));
     *rel = ws.ctl_host[0].rel;

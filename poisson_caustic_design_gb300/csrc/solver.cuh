@@ -90,6 +90,12 @@ int zero_grid(double *phi, int W, int H, int ld, cudaStream_t s);
 // excluded as in the solver) on phi, then ||b - L phi|| / ||b||.
 int smooth_residual(SolverWorkspace &ws, const double *b, double *phi, int W, int H, int ld, int sweeps, double omega,
                     cudaStream_t s, double *rel);
+// The same without the host read: enqueues the sweeps and the residual on
+// caller-owned buffers (mask: H * ld bytes, ctl: one block whose rel field
+// receives the result, partials: residual_partials_bytes()); capturable.
+int enqueue_smooth(const double *b, double *phi, uint8_t *mask, Ctl *ctl, double *partials, int W, int H, int ld,
+                   int sweeps, double omega, cudaStream_t s);
+size_t residual_partials_bytes();
 
 int solve_device(SolverWorkspace &ws, const double *b, double *phi, int W, int H, int ld,
                  const pcd_solve_opts &o, pcd_solve_stats *stats, cudaStream_t s);
