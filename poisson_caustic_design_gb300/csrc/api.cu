@@ -68,30 +68,45 @@ int judge_prepare(pcd_ctx *ctx, int W, int H, int ld, cudaStream_t s)
         if (J.pred) cudaFree(J.pred);
         if (J.zero) cudaFree(J.zero);
         if (J.mask) cudaFree(J.mask);
+        if (J.mask_z) cudaFree(J.mask_z);
         J.b = J.pred = J.zero = nullptr;
-        J.mask = nullptr;
+        J.mask = J.mask_z = nullptr;
         J.cells = 0;
         PCD_CUDA(cudaMalloc(&J.b, cells * sizeof(double)));
         PCD_CUDA(cudaMalloc(&J.pred, cells * sizeof(double)));
         PCD_CUDA(cudaMalloc(&J.zero, cells * sizeof(double)));
         PCD_CUDA(cudaMalloc(&J.mask, cells));
+        PCD_CUDA(cudaMalloc(&J.mask_z, cells));
         J.cells = cells;
     }
     if (!J.ctl) {
         PCD_CUDA(cudaMalloc(&J.ctl, 2 * sizeof(Ctl)));
         PCD_CUDA(cudaMalloc(&J.partials, residual_partials_bytes()));
+        PCD_CUDA(cudaMalloc(&J.partials_z, residual_partials_bytes()));
         PCD_CUDA(cudaMalloc(&J.out, sizeof(JudgeOut)));
         PCD_CUDA(cudaMallocHost(&J.out_host, sizeof(JudgeOut)));
         PCD_CUDA(cudaEventCreateWithFlags(&J.done, cudaEventDisableTiming));
+        PCD_CUDA(cudaEventCreateWithFlags(&J.fork, cudaEventDisableTiming));
+        PCD_CUDA(cudaEventCreateWithFlags(&J.join, cudaEventDisableTiming));
+        PCD_CUDA(cudaStreamCreateWithFlags(&J.side, cudaStreamNonBlocking));
     }
     const unsigned long long n0 = g_launches.load();
     cudaGraph_t g;
     PCD_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-    int st = net.warm_start(J.b, W, H, ld, J.pred, s);
-    if (st == PCD_OK) st = zero_grid(J.zero, W, H, ld, s);
-    if (st == PCD_OK) st = enqueue_smooth(J.b, J.zero, J.mask, J.ctl, J.partials, W, H, ld, kLearnedSmooth, 1.0, s);
+    // the zero guess's smoothing on a side branch (it needs only b), the
+    // prediction and its smoothing on the main one, joined before the end
+    int st = cudaEventRecord(J.fork, s) == cudaSuccess && cudaStreamWaitEvent(J.side, J.fork, 0) == cudaSuccess
+                 ? PCD_OK
+                 : PCD_DEVICE_ERROR;
+    if (st == PCD_OK) st = zero_grid(J.zero, W, H, ld, J.side);
+    if (st == PCD_OK)
+        st = enqueue_smooth(J.b, J.zero, J.mask_z, J.ctl, J.partials_z, W, H, ld, kLearnedSmooth, 1.0, J.side);
+    if (st == PCD_OK && cudaEventRecord(J.join, J.side) != cudaSuccess) st = PCD_DEVICE_ERROR;
+    if (st == PCD_OK) st = net.warm_start(J.b, W, H, ld, J.pred, s);
     if (st == PCD_OK)
         st = enqueue_smooth(J.b, J.pred, J.mask, J.ctl + 1, J.partials, W, H, ld, kLearnedSmooth, 1.0, s);
+    if (st == PCD_OK && cudaStreamWaitEvent(s, J.join, 0) != cudaSuccess) st = PCD_DEVICE_ERROR;
+    if (st == PCD_DEVICE_ERROR) set_error("judge graph: fork / join of the capture failed");
     const cudaError_t ce = cudaStreamEndCapture(s, &g);
     // nothing ran during the capture: count the kernels at each replay instead
     J.launches = g_launches.load() - n0;
@@ -125,8 +140,13 @@ void JudgeGraph::release()
     if (pred) cudaFree(pred);
     if (zero) cudaFree(zero);
     if (mask) cudaFree(mask);
+    if (mask_z) cudaFree(mask_z);
     if (ctl) cudaFree(ctl);
     if (partials) cudaFree(partials);
+    if (partials_z) cudaFree(partials_z);
+    if (side) cudaStreamDestroy(side);
+    if (fork) cudaEventDestroy(fork);
+    if (join) cudaEventDestroy(join);
     if (out) cudaFree(out);
     if (out_host) cudaFreeHost(out_host);
     if (done) cudaEventDestroy(done);

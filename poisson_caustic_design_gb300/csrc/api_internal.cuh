@@ -52,8 +52,10 @@ struct JudgeGraph {
     cudaGraphExec_t exec = nullptr;
     unsigned long long launches = 0;  // kernels per replay
     size_t cells = 0;
-    double *b = nullptr, *pred = nullptr, *zero = nullptr, *partials = nullptr;
-    uint8_t *mask = nullptr;
+    double *b = nullptr, *pred = nullptr, *zero = nullptr, *partials = nullptr, *partials_z = nullptr;
+    uint8_t *mask = nullptr, *mask_z = nullptr;
+    cudaStream_t side = nullptr;    // the zero guess's branch of the capture
+    cudaEvent_t fork = nullptr, join = nullptr;
     Ctl *ctl = nullptr;             // [2]: zero guess, prediction
     JudgeOut *out = nullptr;        // device
     JudgeOut *out_host = nullptr;   // pinned

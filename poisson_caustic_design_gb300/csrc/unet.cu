@@ -22,6 +22,7 @@
 #include <cmath>
 #include <cstring>
 #include <random>
+#include <algorithm>
 #include <vector>
 
 #include "api_internal.cuh"
@@ -226,7 +227,8 @@ int UNet::build(int S_, int maxB_)
     plan.push_back({(void **)&tr_b, bf(maxPK)});
     plan.push_back({(void **)&colD, bf(maxPKf)});
     plan.push_back({(void **)&wflip, bf(256 * round32(9 * 384))});
-    plan.push_back({(void **)&partials, f4(32L * 256 * round32(9 * 384))});
+    partials_cap = 32L * 256 * round32(9 * 384);
+    plan.push_back({(void **)&partials, f4((long)partials_cap)});
     plan.push_back({(void **)&colpart, f4(256L * 384)});
     plan.push_back({(void **)&small, f4(512L * 33)});
     plan.push_back({(void **)&lossbuf, f4(4096)});
@@ -312,12 +314,25 @@ int UNet::conv_fwd(Conv &c, int B, cudaStream_t s)
     g.M = B * c.S * c.S;
     g.N = c.Cout;
     g.K = c.Kp;
-    g.ksplit = 1;
     g.bias = params_f + c.off_b;
     g.relu = c.relu;
     g.Cb = c.out;
     g.ldc = c.ldout;
-    return nn::gemm(g, s, nullptr);
+    // Small grids (the 64² warm start: 2 to 32 output tiles on the coarse
+    // levels): split K so that about 128 CTAs share the reduction, each with
+    // at least two 32-wide k-tiles, partials summed in a fixed order by
+    // nn::gemm (the training forward pass at full batch keeps one split).
+    const int bn = g.N <= 32 ? 32 : (g.N <= 64 ? 64 : 128);
+    const long tiles = (long)((g.N + bn - 1) / bn) * ((g.M + 127) / 128);
+    const int kt = g.K / 32;
+    g.ksplit = 1;
+    if (tiles < 64 && kt >= 4) {
+        const long want = (128 + tiles - 1) / tiles;
+        g.ksplit = (int)std::min<long>(std::min<long>(want, kt / 2), 32);
+        // the split-K partials must fit the shared partial buffer
+        while (g.ksplit > 1 && (size_t)g.ksplit * g.M * g.N > partials_cap) g.ksplit /= 2;
+    }
+    return nn::gemm(g, s, g.ksplit > 1 ? partials : nullptr);
 }
 
 int UNet::forward(int B, cudaStream_t s)
