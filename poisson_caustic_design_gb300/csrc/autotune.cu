@@ -58,7 +58,7 @@ std::vector<TunedSolve> solve_candidates(const pcd_solve_opts &o)
     };
     if (o.precision == PCD_PREC_MIXED && o.stop == PCD_STOP_REL_RESIDUAL) {
         // cluster (when the grid fits): residual-estimate spacing and cycle drop
-        for (int ce : {16, 32, 64}) add(ce, 3e-2, 0, PCD_SCHED_AUTO);
+        for (int ce : {8, 16, 32, 64}) add(ce, 3e-2, 0, PCD_SCHED_AUTO);
         add(32, 1e-1, 0, PCD_SCHED_AUTO);
         // grids beyond one cluster: the persistent and stream schedules with
         // the FP32 sweeps between FP64 refreshes

@@ -50,6 +50,12 @@ struct SolveArgs {
 double resolve_omega(double omega, int W, int H);
 
 // Per-context workspace of the solver; grows on demand.
+// A mixed-precision FP32 cycle hands over to the FP64 stop test once its
+// FP32 residual estimate is below this fraction of the stop tolerance (the
+// estimate's rounding error, ~1e-7 of the cycle's starting residual, is far
+// below the margin; a cycle that ends just short runs one more check).
+constexpr double kFp32StopFrac = 0.9;
+
 struct SolverWorkspace {
     int dev = 0;
     size_t cells = 0;           // capacity in elements of the per-cell buffers

@@ -153,7 +153,7 @@ __global__ void __launch_bounds__(kBatchThreads, 1) k_sor_batch(BatchArgs a)
         bool converged = rel <= I.tol;
         int sweeps = 0, cycles = 0;
         while (!converged && sweeps < I.max_iter) {
-            const double stop_abs = 0.5 * I.tol * bnorm;
+            const double stop_abs = kFp32StopFrac * I.tol * bnorm;
             const double drop_abs = a.drop * sqrt(r2);
             int cyc = 0;
             for (;;) {

@@ -20,7 +20,7 @@
 // after a barrier and take the same exit decision, so they execute the same
 // sequence of barriers.  A cycle ends when that estimate has dropped by
 // `drop` (the FP32 iteration cannot resolve much more than two digits of the
-// correction) or is below half the stop tolerance, or at the sweep caps; the
+// correction) or is below 0.9 of the stop tolerance, or at the sweep caps; the
 // FP64 residual then decides convergence.
 #include <algorithm>
 #include <cooperative_groups.h>
@@ -67,7 +67,7 @@ __global__ void __launch_bounds__(kClusterThreads, 1) k_sor_cluster(ClusterArgs 
     const int done_before = *(volatile const int *)&ctl->sweeps;
     const double bnorm = *(volatile const double *)&ctl->bnorm;
     const double rstart = *(volatile const double *)&ctl->rnorm;
-    const double stop_abs = 0.5 * a.tol * bnorm;       // verify in FP64 below this
+    const double stop_abs = kFp32StopFrac * a.tol * bnorm;  // verify in FP64 below this
     const double drop_abs = a.drop * rstart;
     // thread -> (slot quad, row group)
     const int KH4 = P.KHp >> 2;
@@ -390,7 +390,7 @@ __global__ void __launch_bounds__(kClusterThreads, 1) k_sor_cluster_tb(ClusterAr
     const int done_before = *(volatile const int *)&ctl->sweeps;
     const double bnorm = *(volatile const double *)&ctl->bnorm;
     const double rstart = *(volatile const double *)&ctl->rnorm;
-    const double stop_abs = 0.5 * a.tol * bnorm;
+    const double stop_abs = kFp32StopFrac * a.tol * bnorm;
     const double drop_abs = a.drop * rstart;
     const int KH4 = KHp >> 2;
     const int RP = blockDim.x / KH4;

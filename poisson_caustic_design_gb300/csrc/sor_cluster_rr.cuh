@@ -313,7 +313,7 @@ __global__ void __launch_bounds__(kRRThreads, 1) k_sor_cluster_rr(ClusterArgs a)
     const int done_before = *(volatile const int *)&ctl->sweeps;
     const double bnorm = *(volatile const double *)&ctl->bnorm;
     const double rstart = *(volatile const double *)&ctl->rnorm;
-    const double stop_abs = 0.5 * a.tol * bnorm;
+    const double stop_abs = kFp32StopFrac * a.tol * bnorm;
     const double drop_abs = a.drop * rstart;
     const double stop2 = stop_abs * stop_abs, drop2 = drop_abs * drop_abs;
     const int P = (st.ybase + w * L) & 1;
