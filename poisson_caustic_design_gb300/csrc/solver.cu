@@ -92,14 +92,15 @@ __device__ __forceinline__ T omega_over_cnt(const SolveArgs &a, int cnt)
     return (T)(cnt == 4 ? a.w32[4] : cnt == 3 ? a.w32[3] : cnt == 2 ? a.w32[2] : cnt == 1 ? a.w32[1] : a.w32[0]);
 }
 
-// End-of-sweep bookkeeping, run by the last block of the black half sweep.
-__device__ void end_of_sweep(Ctl *ctl, const SolveArgs &a)
+// End-of-sweep bookkeeping, run by the last block of the black half sweep
+// (n sweeps done by a kernel that runs several).
+__device__ void end_of_sweep(Ctl *ctl, const SolveArgs &a, int n = 1)
 {
     volatile Ctl *c = ctl;
     unsigned long long bits = atomicExch(&ctl->maxbits, 0ull);
     double mx = __longlong_as_double((long long)bits);
     c->last_max = mx;
-    int s = c->sweeps + 1;
+    int s = c->sweeps + n;
     c->sweeps = s;
     if (a.stop == PCD_STOP_MAX_UPDATE && mx < a.tol) {
         c->converged = 1;
@@ -439,6 +440,7 @@ inline int stripe_rows(int H, int resident)
 }
 
 #include "sor_stream.cuh"
+#include "sor_stream2.cuh"
 
 // Launch shape of the ping-pong stream sweep: G 4-cell groups per thread,
 // T threads (one row of the grid per block), ns stripes of R rows; rows
@@ -448,6 +450,8 @@ struct StreamPlan {
     int G = 0, T = 0, R = 0, ns = 0;
     int tma = 0, wpad = 0;
     size_t smem = 0;
+    int two = 0;          // two sweeps per pass (k_sweep2_tma) available
+    size_t smem2 = 0;
 };
 
 int stream_plan(int dev, int W, int H, int ld, bool allow_tma, StreamPlan *p)
@@ -487,10 +491,42 @@ int stream_plan(int dev, int W, int H, int ld, bool allow_tma, StreamPlan *p)
     p->tma = tma ? 1 : 0;
     p->wpad = wpad;
     p->smem = tma ? smem : 0;
+    // the two-sweep pass: whole 4G-cell groups (W a multiple of 4G, one
+    // group column per thread), one block per SM, stripes of >= 8 rows
+    const size_t smem2 = tma2_smem_bytes(wpad, T);
+    p->two = 0;
+    p->smem2 = 0;
+    if (tma && W % (4 * G) == 0 && T * 4 * G == W && smem2 + 1024 <= (size_t)max_smem && p->R >= 8) {
+        const void *fns2[2] = {G == 1 ? (const void *)k_sweep2_tma<1, false> : (const void *)k_sweep2_tma<2, false>,
+                               G == 1 ? (const void *)k_sweep2_tma<1, true> : (const void *)k_sweep2_tma<2, true>};
+        int ok2 = 1;
+        for (const void *fn : fns2) {
+            PCD_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem2));
+            int b2 = 0;
+            PCD_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b2, fn, T, smem2));
+            if (b2 < 1) ok2 = 0;
+        }
+        if (ok2) {
+            p->two = 1;
+            p->smem2 = smem2;
+        }
+    }
     return PCD_OK;
 }
 
 constexpr long kTmaSpinLimit = 1l << 22;
+
+// Two sweeps from ein into eout (one when a single sweep is left before
+// max_iter).
+template <bool TRACK>
+void launch_stream2_t(const StreamPlan &p, const float *ein, float *eout, const float *r, Ctl *ctl,
+                      const SolveArgs &a, int out_idx, cudaStream_t s)
+{
+    if (p.G == 1)
+        k_sweep2_tma<1, TRACK><<<p.ns, p.T, p.smem2, s>>>(ein, eout, r, ctl, a, p.R, out_idx, p.wpad, kTmaSpinLimit);
+    else
+        k_sweep2_tma<2, TRACK><<<p.ns, p.T, p.smem2, s>>>(ein, eout, r, ctl, a, p.R, out_idx, p.wpad, kTmaSpinLimit);
+}
 
 template <bool TRACK>
 void launch_stream_t(const StreamPlan &p, const float *ein, float *eout, const float *r, Ctl *ctl, const SolveArgs &a,
@@ -641,13 +677,23 @@ int enqueue_chunk(SolverWorkspace &ws, const double *b, double *phi, const Solve
         sweeps = 0;
     }
     if (!MASKED && sched == PCD_SCHED_STREAM) {
-        // sweep k reads buffer k&1 and writes the other; the settle kernel
-        // moves the latest correction into e32 for the refinement
-        for (int k = 0; k < sweeps; k++) {
+        // launch k reads buffer k&1 and writes the other (two sweeps per
+        // launch where the plan allows, a single sweep for an odd rest); the
+        // settle kernel moves the latest correction into e32 for the refinement
+        int k = 0;
+        for (int done = 0; done < sweeps; k++) {
             const float *ein = (k & 1) ? ws.e32b : ws.e32;
             float *eout = (k & 1) ? ws.e32 : ws.e32b;
-            if (track) launch_stream_t<true>(sp, ein, eout, ws.r32, ws.ctl, a, (k & 1) ? 0 : 1, s);
-            else launch_stream_t<false>(sp, ein, eout, ws.r32, ws.ctl, a, (k & 1) ? 0 : 1, s);
+            const int out = (k & 1) ? 0 : 1;
+            if (sp.two && sweeps - done >= 2) {
+                if (track) launch_stream2_t<true>(sp, ein, eout, ws.r32, ws.ctl, a, out, s);
+                else launch_stream2_t<false>(sp, ein, eout, ws.r32, ws.ctl, a, out, s);
+                done += 2;
+            } else {
+                if (track) launch_stream_t<true>(sp, ein, eout, ws.r32, ws.ctl, a, out, s);
+                else launch_stream_t<false>(sp, ein, eout, ws.r32, ws.ctl, a, out, s);
+                done += 1;
+            }
             n++;
         }
         k_stream_settle<<<rblocks, kThreads, 0, s>>>(ws.e32, ws.e32b, ws.ctl, a);
@@ -689,7 +735,7 @@ int get_chunk_graph(SolverWorkspace &ws, const double *b, double *phi, const Sol
                     const StreamPlan &sp)
 {
     std::vector<long long> key = {(long long)(uintptr_t)b, (long long)(uintptr_t)phi, a.W, a.H, a.ld, a.stop,
-                                  a.max_iter, precision, masked, sweeps, sched, sp.G, sp.T, sp.R, sp.tma};
+                                  a.max_iter, precision, masked, sweeps, sched, sp.G, sp.T, sp.R, sp.tma, sp.two};
     long long tb, ob;
     std::memcpy(&tb, &a.tol, 8);
     std::memcpy(&ob, &a.omega, 8);
