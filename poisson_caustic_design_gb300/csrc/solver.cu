@@ -483,7 +483,9 @@ int stream_plan(int dev, int W, int H, int ld, bool allow_tma, StreamPlan *p)
     if (bps < 1) return PCD_BAD_ARG;
     int ns = std::min(bps * sms, ceil_div(H, kStreamRowsMin));
     if (ns < 1) ns = 1;
-    const int R = ceil_div(H, ns);
+    // even stripe heights: every stripe starts on an even row (the two-sweep
+    // pass relies on it for its compile-time cell parities)
+    const int R = 2 * ceil_div(ceil_div(H, ns), 2);
     p->G = G;
     p->T = T;
     p->R = R;
@@ -496,7 +498,8 @@ int stream_plan(int dev, int W, int H, int ld, bool allow_tma, StreamPlan *p)
     const size_t smem2 = tma2_smem_bytes(wpad, T);
     p->two = 0;
     p->smem2 = 0;
-    if (tma && W % (4 * G) == 0 && T * 4 * G == W && smem2 + 1024 <= (size_t)max_smem && p->R >= 8) {
+    if (tma && W % (4 * G) == 0 && T * 4 * G == W && smem2 + 1024 <= (size_t)max_smem && p->R >= 8 &&
+        p->R % 2 == 0) {
         const void *fns2[2] = {G == 1 ? (const void *)k_sweep2_tma<1, false> : (const void *)k_sweep2_tma<2, false>,
                                G == 1 ? (const void *)k_sweep2_tma<1, true> : (const void *)k_sweep2_tma<2, true>};
         int ok2 = 1;

@@ -20,7 +20,9 @@
 // update, and the right-hand side rows y-3 .. y read from their ring slots.
 // Horizontal neighbours of updated cells across threads go through a small
 // shared array of each thread's first and last cell per updated row
-// (double-buffered by step), so one block barrier per step suffices.
+// (double-buffered by step), so one block barrier per step suffices; those
+// of the input row come from the adjacent lanes.  Stripes start on even rows,
+// which makes every cell parity a compile-time constant of the step.
 // Rows arrive by cp.async.bulk into two rings with one mbarrier per slot:
 // the input ring (4 rows, filled 2 steps ahead) and the right-hand side ring
 // (8 rows: a row is read in 4 consecutive steps, filled 4 steps ahead).
@@ -69,8 +71,13 @@ __device__ __forceinline__ bool tma2_step(float4 (&Wn)[6][G], float (&edg)[2][2]
             const float *src = es + (size_t)(t & (kE2 - 1)) * wpad;
 #pragma unroll
             for (int k = 0; k < G; k++) dst[k] = *reinterpret_cast<const float4 *>(src + col0 + 4 * k);
-            lft = col0 > 0 ? src[col0 - 1] : 0.f;
-            rgt = col0 + 4 * G < W ? src[col0 + 4 * G] : 0.f;
+            // outer neighbours from the adjacent lanes; the warp's end lanes
+            // read theirs from the slot
+            const int lane = tid & 31;
+            lft = __shfl_up_sync(0xffffffffu, dst[G - 1].w, 1);
+            rgt = __shfl_down_sync(0xffffffffu, dst[0].x, 1);
+            if (lane == 0) lft = col0 > 0 ? src[col0 - 1] : 0.f;
+            if (lane == 31) rgt = col0 + 4 * G < W ? src[col0 + 4 * G] : 0.f;
         } else {
 #pragma unroll
             for (int k = 0; k < G; k++) dst[k] = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -92,9 +99,13 @@ __device__ __forceinline__ bool tma2_step(float4 (&Wn)[6][G], float (&edg)[2][2]
         if (rr <= r_last) tma_row(rs + (size_t)((j + 4) & (kR2 - 1)) * wpad, rhs + (long)rr * ld, bytes,
                                   rbar + ((j + 4) & (kR2 - 1)));
     }
-    const int par = y & 1;  // column parity of the red cells of y, y-2 and the black cells of y-1, y-3
-    float *xw = xb + (size_t)(P & 1) * 3 * T * 2;        // written at this step
-    const float *xr = xb + (size_t)((P + 1) & 1) * 3 * T * 2;  // written at step j-1
+    // column parity of the red cells of y, y-2 and the black cells of y-1,
+    // y-3: y0 is even (the plan gives even stripe heights), so y & 1 =
+    // (P + 1) & 1
+    constexpr int par = (P + 1) & 1;
+    // boundary cells [buffer][kind][first / last][thread]
+    float *xw = xb + (size_t)(P & 1) * 3 * 2 * T;              // written at this step
+    const float *xr = xb + (size_t)((P + 1) & 1) * 3 * 2 * T;  // written at step j-1
     const bool lo_ok = tid > 0, hi_ok = tid + 1 < T;
     auto rhs_row = [&](int jr, float4 (&r)[G]) {
         const float *src = rs + (size_t)(jr & (kR2 - 1)) * wpad;
@@ -102,8 +113,8 @@ __device__ __forceinline__ bool tma2_step(float4 (&Wn)[6][G], float (&edg)[2][2]
         for (int k = 0; k < G; k++) r[k] = *reinterpret_cast<const float4 *>(src + col0 + 4 * k);
     };
     auto publish = [&](int kind, const float4 (&c)[G]) {
-        xw[((size_t)kind * T + tid) * 2] = c[0].x;
-        xw[((size_t)kind * T + tid) * 2 + 1] = c[G - 1].w;
+        xw[(size_t)(2 * kind) * T + tid] = c[0].x;
+        xw[(size_t)(2 * kind + 1) * T + tid] = c[G - 1].w;
     };
     auto store = [&](int row, const float4 (&c)[G]) {
 #pragma unroll
@@ -127,8 +138,8 @@ __device__ __forceinline__ bool tma2_step(float4 (&Wn)[6][G], float (&edg)[2][2]
     if (y1b >= max(y0 - 2, 0) && y1b <= min(y1 + 1, H - 1)) {
         float4 r[G];
         rhs_row(j - 1, r);
-        const float lft = lo_ok ? xr[((size_t)0 * T + tid - 1) * 2 + 1] : 0.f;
-        const float rgt = hi_ok ? xr[((size_t)0 * T + tid + 1) * 2] : 0.f;
+        const float lft = lo_ok ? xr[(size_t)1 * T + tid - 1] : 0.f;
+        const float rgt = hi_ok ? xr[(size_t)0 * T + tid + 1] : 0.f;
         if (TRACK && !two && y1b >= y0 && y1b < y1)
             relax_row_groups<G, true>(Wn[wA1], Wn[wA2], Wn[w0], r, lft, rgt, col0, y1b, W, H, par, w, m);
         else
@@ -142,8 +153,8 @@ __device__ __forceinline__ bool tma2_step(float4 (&Wn)[6][G], float (&edg)[2][2]
     if (y2r >= max(y0 - 1, 0) && y2r <= min(y1, H - 1)) {
         float4 r[G];
         rhs_row(j - 2, r);
-        const float lft = lo_ok ? xr[((size_t)1 * T + tid - 1) * 2 + 1] : 0.f;
-        const float rgt = hi_ok ? xr[((size_t)1 * T + tid + 1) * 2] : 0.f;
+        const float lft = lo_ok ? xr[(size_t)3 * T + tid - 1] : 0.f;
+        const float rgt = hi_ok ? xr[(size_t)2 * T + tid + 1] : 0.f;
         if (TRACK && y2r >= y0 && y2r < y1)
             relax_row_groups<G, true>(Wn[wA2], Wn[wA3], Wn[wA1], r, lft, rgt, col0, y2r, W, H, par, w, m);
         else
@@ -155,8 +166,8 @@ __device__ __forceinline__ bool tma2_step(float4 (&Wn)[6][G], float (&edg)[2][2]
     if (y2b >= max(y0, 0) && y2b <= min(y1 - 1, H - 1)) {
         float4 r[G];
         rhs_row(j - 3, r);
-        const float lft = lo_ok ? xr[((size_t)2 * T + tid - 1) * 2 + 1] : 0.f;
-        const float rgt = hi_ok ? xr[((size_t)2 * T + tid + 1) * 2] : 0.f;
+        const float lft = lo_ok ? xr[(size_t)5 * T + tid - 1] : 0.f;
+        const float rgt = hi_ok ? xr[(size_t)4 * T + tid + 1] : 0.f;
         relax_row_groups<G, TRACK>(Wn[wA3], Wn[wA4], Wn[wA2], r, lft, rgt, col0, y2b, W, H, par, w, m);
         store(y2b, Wn[wA3]);
     }
