@@ -383,8 +383,13 @@ def run_ours(args, rank, world, local, pg):
     alg_bytes = 12.0 * cells * hm["sweeps"]
     achieved = alg_bytes / (hm["sweep_ms"] * 1e-3) / 1e9
     peak, peak_src = measured_hbm_peak()
+    # DRAM bytes of one k_sor_cluster_rr launch (one FP32 cycle, ~430 sweeps
+    # at 512^2) from the ncu capture summarised in
+    # profiles/k_sor_cluster_rr_512_full.md: the band load of e and r32 (the
+    # store stays in L2), against ~1.35 GB of algorithmic bytes per launch
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-            "traffic": None, "peak_source": peak_src,
+            "traffic": 2.164992e6, "traffic_unit": "bytes per launch (ncu)",
+            "alg_bytes_per_launch": 12.0 * cells * 430, "peak_source": peak_src,
             "kernel": "k_sor_cluster_rr (FP32 sweeps)", "alg_bytes_per_solve": alg_bytes,
             "note": "the 512^2 working set stays on one 16-CTA cluster for a whole FP32 cycle (e in registers, "
                     "r32 in shared memory): the kernel is bound by FP32 issue, block and cluster barriers, not "
