@@ -101,10 +101,11 @@ def test_stripes_on_grid_beyond_chip(ctx, prec):
 @pytest.mark.parametrize("n,m,ld", [(2048, 1800, 2048), (4096, 300, 4096), (1000, 37, 1000), (1001, 50, 1004),
                                     (128, 3, 128), (4093, 40, 4096)])
 def test_stream_sweeps_match_launch_schedule(ctx, n, m, ld):
-    """The ping-pong stream sweeps (one pass per sweep from one FP32 buffer
-    into the other, stripe-edge red rows recomputed) run the same red-black
-    iteration as the launch-per-half-sweep kernels: after the same odd number
-    of mixed-precision sweeps (the last one lands in the second buffer) the
+    """The ping-pong stream sweeps (two sweeps per pass from one FP32 buffer
+    into the other where the width is whole 4-cell groups, one per pass
+    otherwise; the stripes' dependency cones recomputed) run the same
+    red-black iteration as the launch-per-half-sweep kernels: after the same
+    odd number of mixed-precision sweeps (the last pass a single sweep) the
     iterates agree to FP32 rounding.  Covers one and two 4-cell groups per
     thread, partial last groups (width not a multiple of 4) and short grids."""
     import torch
@@ -124,6 +125,47 @@ def test_stream_sweeps_match_launch_schedule(ctx, n, m, ld):
     assert np.isfinite(out[5]).all()
     err = np.abs(out[5] - out[1]).max() / np.abs(out[1]).max()
     assert err < 1e-5, err
+
+
+def test_stream_two_sweep_pass_stops_at_max_iterations(ctx):
+    """A two-sweep pass launched with one sweep left before max_iterations
+    (chunks of 4 sweeps, 37 sweeps) runs a single sweep: the sweep count and
+    the iterate match the launch schedule with the same FP64 refreshes."""
+    import poisson_caustic_design_gb300 as pcd
+
+    b = pcd.inputs.poisson_rhs(1024, 5, "gaussian", m=300)
+    out = {}
+    for sched in (1, 5):
+        phi = np.zeros_like(b)
+        st = ctx.solve(b, phi, pcd.SolveOptions(stop=pcd.STOP_REL_RESIDUAL, tol=0.0, max_iterations=37,
+                                                precision=pcd.PREC_MIXED, omega=-1.0, schedule=sched,
+                                                refine_every=4))
+        assert st["sweeps"] == 37 and st["schedule_used"] == sched
+        out[sched] = phi
+    err = np.abs(out[5] - out[1]).max() / np.abs(out[1]).max()
+    assert err < 1e-5, err
+
+
+def test_stream_max_update_stop_matches_plain(ctx):
+    """The reference's stop rule (max |delta| of a sweep below the threshold)
+    on the stream schedule, where the two-sweep pass tracks its last sweep:
+    the mixed solve stops within a few sweeps of the plain FP64 one and both
+    land equally close to the exact solution."""
+    import oracle
+    import poisson_caustic_design_gb300 as pcd
+
+    b = pcd.inputs.poisson_rhs(1024, 6, "gaussian", m=256)
+    exact = oracle.dct_solve(b)
+    res = {}
+    for name, prec, sched in (("plain", pcd.PREC_FP64, 1), ("mixed", pcd.PREC_MIXED, 5)):
+        phi = np.zeros_like(b)
+        st = ctx.solve(b, phi, pcd.SolveOptions(stop=pcd.STOP_MAX_UPDATE, tol=1e-7, max_iterations=200000,
+                                                precision=prec, omega=-1.0, schedule=sched))
+        assert st["converged"] and st["schedule_used"] == sched
+        res[name] = (st["sweeps"], _rel_mod_const(phi, exact)[0])
+    (sp, ep), (sm, em) = res["plain"], res["mixed"]
+    assert abs(sm - sp) <= 0.03 * sp, (sp, sm)
+    assert em <= 1.5 * ep + 1e-9, (ep, em)
 
 
 @pytest.mark.parametrize("n,m", [(512, 512), (96, 80), (640, 480), (33, 17), (1024, 300), (1024, 400), (256, 256),

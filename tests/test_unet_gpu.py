@@ -170,6 +170,40 @@ def test_learned_warm_start_policy(ctx):
     net.close()
 
 
+def test_judge_graph_follows_inputs(ctx):
+    """The learned warm start and its judge replay one captured graph per
+    shape on the context's own buffers: each solve judges its own b (the
+    same verdict and residuals as on a fresh context), across repeated,
+    alternating and reshaped inputs."""
+    import torch
+
+    import poisson_caustic_design_gb300 as pcd
+    from poisson_caustic_design_gb300 import learned
+
+    def judged(c, b):
+        phi = torch.zeros_like(b)
+        st = c.solve_device(b, phi, pcd.SolveOptions(stop=pcd.STOP_REL_RESIDUAL, tol=1e-6, precision=pcd.PREC_MIXED,
+                                                     omega=-1.0, warm_start=2))
+        assert st["converged"] and st["warm_used"] in (2, 3)
+        return st["warm_used"], st["warm_rel_residual"], st["warm_zero_rel_residual"]
+
+    bs = [torch.from_numpy(pcd.inputs.poisson_rhs(n, s, "gaussian", m=m)).cuda()
+          for n, m, s in ((128, 128, 3), (128, 128, 4), (96, 80, 5))]
+    net = learned.UNet(ctx, resolution=64, max_batch=1, seed=11)
+    net.attach(ctx)
+    seq = [judged(ctx, bs[i]) for i in (0, 1, 0, 2, 1)]
+    assert seq[0] == seq[2] and seq[1] == seq[4]
+    assert seq[0][2] != seq[1][2]
+    other = pcd.Context(0)
+    net2 = learned.UNet(other, resolution=64, max_batch=1, seed=11)
+    net2.attach(other)
+    assert judged(other, bs[1]) == seq[1]
+    assert judged(other, bs[2]) == seq[3]
+    net2.close()
+    other.close()
+    net.close()
+
+
 def test_trained_network_gains_over_zero_guess(ctx):
     """With the committed trained weights (a 64^2 network trained on 20k
     256^2 pairs) the learned warm start is kept on most held-out 256^2 and
