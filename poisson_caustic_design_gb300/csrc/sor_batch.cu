@@ -197,6 +197,9 @@ __global__ void __launch_bounds__(kBatchThreads, 1) k_sor_batch(BatchArgs a)
 int BatchWorkspace::reserve_inst(int count)
 {
     if (count > cap) {
+        // cached graphs hold the old descriptor addresses: drop them with them
+        for (auto &kv : graphs) cudaGraphExecDestroy(kv.second);
+        graphs.clear();
         if (d_inst) cudaFree(d_inst);
         if (h_inst) cudaFreeHost(h_inst);
         d_inst = nullptr;
@@ -302,6 +305,9 @@ int batch_solve_device(BatchWorkspace &ws, int dev, const pcd_instance *inst, in
     }
     ncl = std::min(ncl, count);
     if (gper * ncl > ws.gscratch_floats) {
+        // cached graphs hold the old scratch address: drop them with it
+        for (auto &kv : ws.graphs) cudaGraphExecDestroy(kv.second);
+        ws.graphs.clear();
         if (ws.gscratch) cudaFree(ws.gscratch);
         ws.gscratch = nullptr;
         ws.gscratch_floats = 0;

@@ -220,45 +220,52 @@ __device__ __forceinline__ float4 quad_row_edge(float4 v, const float4 &rh, cons
 }
 
 // One half sweep of colour c over plane rows [lo, hi) with four slots per
-// thread: slots k..k+3 (k a multiple of 4) of rows lo + rg, lo + rg + RP, ...
-// (grid row y = ybase + lr; rows outside the grid are skipped; threads with
-// rg >= RP idle).  rhs row lr sits at rhs + lr * KHp + roff.  Five 16-byte
-// shared loads and one store per four cells.  In rows other than the grid's
-// first and last only the first quad (x0 = 0) and the last quad (x0 + 7 >= W)
-// have cells without four neighbours: one lane per row and colour takes the
-// short edge form, the first and last grid rows take the general form on
-// all their lanes.  Reads of slot k-1 at k = 0 and of slot KHp at k = KHp-4
-// fall in the previous / next plane row (both exist) and are used only for
-// cells without that neighbour.
-__device__ __forceinline__ void relax_rows_quad(float *__restrict__ own, const float *__restrict__ oth,
-                                                const float *__restrict__ rhs, long roff, int c, int lo, int hi,
-                                                int ybase, const Grid &G, int KHp, int k, int rg, int RP)
+// thread: slots k..k+3 (k a multiple of 4); row group rg walks the rows
+// [lo + rg L, lo + rg L + L) top-down (grid row y = ybase + lr; rows outside
+// the grid are skipped; threads with rg >= RP idle), keeping the other
+// colour's rows lr-1, lr, lr+1 in registers from one row to the next (one
+// new 16-byte load of them per row), which matters where the planes live in
+// L2.  rhs row lr sits at rhs + lr * KHp + roff.  In rows other than the
+// grid's first and last only the first quad (x0 = 0) and the last quad
+// (x0 + 7 >= W) have cells without four neighbours: they take the short edge
+// form, the first and last grid rows the general form.  Reads of slot k-1
+// at k = 0 and of slot KHp at k = KHp-4 fall in the previous / next plane
+// row (both exist) and are used only for cells without that neighbour.
+__device__ __forceinline__ void relax_block_quad(float *__restrict__ own, const float *__restrict__ oth,
+                                                 const float *__restrict__ rhs, long roff, int c, int lo, int hi,
+                                                 int ybase, const Grid &G, int KHp, int k, int rg, int RP)
 {
     const int W = G.W, H = G.H;
     const float w4 = G.w4;
     if (rg >= RP) return;
+    const int L = (hi - lo + RP - 1) / RP;
+    const int b0 = lo + rg * L, b1 = min(b0 + L, hi);
+    if (b0 >= b1) return;
+    float4 up = *reinterpret_cast<const float4 *>(oth + (size_t)(b0 - 1) * KHp + k);
+    float4 mid = *reinterpret_cast<const float4 *>(oth + (size_t)b0 * KHp + k);
 #pragma unroll 1
-    for (int lr = lo + rg; lr < hi; lr += RP) {
-        const int y = ybase + lr;
-        if (y < 0 || y >= H) continue;
-        const int s = (y & 1) ^ c;   // x = 2 * slot + s
-        const int q = 1 - s;         // left neighbour slot = slot - q
-        const int x0 = 2 * k + s;
+    for (int lr = b0; lr < b1; lr++) {
         const size_t ro = (size_t)lr * KHp;
-        const float4 v = *reinterpret_cast<const float4 *>(own + ro + k);
-        const float4 rh = *reinterpret_cast<const float4 *>(rhs + ro + roff + k);
-        const float4 up = *reinterpret_cast<const float4 *>(oth + ro - KHp + k);
         const float4 dn = *reinterpret_cast<const float4 *>(oth + ro + KHp + k);
-        const float4 mid = *reinterpret_cast<const float4 *>(oth + ro + k);
-        const float extra = oth[ro + (q ? k - 1 : k + 4)];
-        float4 nv;
-        if (y > 0 && y < H - 1) {
-            if (x0 > 0 && x0 + 7 < W) nv = quad_interior(v, rh, up, dn, mid, extra, q, w4);
-            else nv = quad_row_edge(v, rh, up, dn, mid, extra, q, x0, W, G.w2, G.w3, w4);
-        } else {
-            nv = quad_general(v, rh, up, dn, mid, extra, q, x0, y, W, H, G.w0, G.w1, G.w2, G.w3, w4);
+        const int y = ybase + lr;
+        if (y >= 0 && y < H) {
+            const int s = (y & 1) ^ c;
+            const int q = 1 - s;
+            const int x0 = 2 * k + s;
+            const float4 v = *reinterpret_cast<const float4 *>(own + ro + k);
+            const float4 rh = *reinterpret_cast<const float4 *>(rhs + ro + roff + k);
+            const float extra = oth[ro + (q ? k - 1 : k + 4)];
+            float4 nv;
+            if (y > 0 && y < H - 1) {
+                if (x0 > 0 && x0 + 7 < W) nv = quad_interior(v, rh, up, dn, mid, extra, q, w4);
+                else nv = quad_row_edge(v, rh, up, dn, mid, extra, q, x0, W, G.w2, G.w3, w4);
+            } else {
+                nv = quad_general(v, rh, up, dn, mid, extra, q, x0, y, W, H, G.w0, G.w1, G.w2, G.w3, w4);
+            }
+            *reinterpret_cast<float4 *>(own + ro + k) = nv;
         }
-        *reinterpret_cast<float4 *>(own + ro + k) = nv;
+        up = mid;
+        mid = dn;
     }
 }
 
@@ -287,7 +294,8 @@ __device__ __forceinline__ float quad_residual_sq(const float4 &v, const float4 
 }
 
 // Sum over plane rows [lo, hi) (grid row ybase + lr), both colours, of
-// (r - L e)^2 in FP32 per thread; the same quad mapping as relax_rows_quad.
+// (r - L e)^2 in FP32 per thread; the same slot mapping as relax_block_quad
+// with the rows taken round-robin over the row groups.
 __device__ __forceinline__ float residual_rows_quad(const float *__restrict__ e0, const float *__restrict__ e1,
                                                    const float *__restrict__ r0p, const float *__restrict__ r1p,
                                                    long roff, int lo, int hi, int ybase, const Grid &G, int KHp,
@@ -363,7 +371,7 @@ __device__ __forceinline__ void cluster_sum2(cg::cluster_group &cl, double *s_pa
 // One half sweep of colour c over the band (plane rows 1..n, rhs rows 0..n-1).
 __device__ __forceinline__ void relax_quad(const Planes &P, int c, int n, int r0, const Grid &G, int k, int rg, int RP)
 {
-    relax_rows_quad(P.e(c), P.e(c ^ 1), P.r(c), -(long)P.KHp, c, 1, n + 1, r0 - 1, G, P.KHp, k, rg, RP);
+    relax_block_quad(P.e(c), P.e(c ^ 1), P.r(c), -(long)P.KHp, c, 1, n + 1, r0 - 1, G, P.KHp, k, rg, RP);
 }
 
 // Block-wide sum into thread 0 (blockDim a multiple of 32).

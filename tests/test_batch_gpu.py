@@ -55,6 +55,39 @@ def test_batch_graph_replay_is_repeatable(ctx):
     assert [x["sweeps"] for x in per1] == [x["sweeps"] for x in per2]
 
 
+def test_batch_graphs_survive_buffer_growth():
+    """A cached batch graph holds the addresses of the context's scratch and
+    descriptor buffers: a later batch that needs more of either reallocates
+    them and drops the cached graphs, so replaying the first batch's
+    signature captures it again (same results as on a fresh context)."""
+    import torch
+
+    import poisson_caustic_design_gb300 as pcd
+
+    opts = pcd.SolveOptions(stop=pcd.STOP_REL_RESIDUAL, tol=1e-6, max_iterations=200000, omega=-1.0,
+                            warm_start=False)
+    small = [torch.from_numpy(pcd.inputs.poisson_rhs(1024, 61, "gaussian", m=512)).cuda()]
+    large = [torch.from_numpy(pcd.inputs.poisson_rhs(1024, 62 + i, "gaussian")).cuda() for i in range(3)]
+    large += [torch.from_numpy(pcd.inputs.poisson_rhs(64, 70 + i, "binary")).cuda() for i in range(40)]
+
+    def run(c, bs):
+        ps = [torch.zeros_like(b) for b in bs]
+        per, bst = pcd.batch_solve(c, bs, ps, opts)
+        torch.cuda.synchronize()
+        assert bst["status"] == 0 and all(x["converged"] for x in per)
+        return [p.cpu() for p in ps]
+
+    ctx = pcd.Context(0)
+    first = run(ctx, small)
+    run(ctx, large)          # more global scratch and more descriptors
+    again = run(ctx, small)  # the first signature again
+    ctx.close()
+    fresh_ctx = pcd.Context(0)
+    fresh = run(fresh_ctx, small)
+    fresh_ctx.close()
+    assert torch.equal(first[0], again[0]) and torch.equal(first[0], fresh[0])
+
+
 def test_batch_rejects_bad_instances(ctx):
     import torch
 
