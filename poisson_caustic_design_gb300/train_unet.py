@@ -69,7 +69,7 @@ def summarize(rows):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--out", required=True)
+    ap.add_argument("--out", default=None, help="where to write the trained weights (required unless --evaluate-only)")
     ap.add_argument("--pairs", type=int, default=20000)
     ap.add_argument("--resolution", type=int, default=64, help="network grid")
     ap.add_argument("--data-resolution", type=int, default=256, help="grid of the training solves")
@@ -82,6 +82,8 @@ def main():
     ap.add_argument("--evaluate-only", default=None, metavar="WEIGHTS",
                     help="skip training: evaluate these weights on the held-out seeds")
     args = ap.parse_args()
+    if not args.evaluate_only and not args.out:
+        ap.error("--out is required unless --evaluate-only is given")
 
     import torch
 
