@@ -205,7 +205,7 @@ def test_judge_graph_follows_inputs(ctx):
 
 
 def test_trained_network_gains_over_zero_guess(ctx):
-    """With the committed trained weights (a 64^2 network trained on 20k
+    """With the committed trained weights (a 64^2 network trained on 40k
     256^2 pairs) the learned warm start is kept on most held-out 256^2 and
     512^2 densities (Gaussian mixtures and binary shapes) and the solves to
     relative residual 1e-6 need fewer sweeps on average than from a zero guess
