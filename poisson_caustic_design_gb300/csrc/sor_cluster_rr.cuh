@@ -2,10 +2,12 @@
 // (included by sor_cluster.cu inside its anonymous namespace, after the
 // shared-memory helpers lds4 / sts4).
 //
-// Widths W = 8 KQ up to 512.  A CTA of 16 warps; warp w holds the plane rows
-// [w L, w L + L) of the CTA's band plus halo, lane l the quads qi = l + 32 i
-// (i < NQ) of both colours of each of its rows in registers: quad qi of
-// colour c in row y covers the cells x = 8 qi + 2 t + ((y & 1) ^ c), t < 4.
+// Widths W = 8 KQ up to 512, K = 4 or 2 sweeps per halo exchange, L = 2..4
+// rows per warp, NQ = 1 or 2 quads per lane.  A CTA of 16 warps; warp w
+// holds the plane rows [w L, w L + L) of the CTA's band plus halo, lane l the
+// quads qi = l + 32 i (i < NQ) of both colours of each of its rows in
+// registers: quad qi of colour c in row y covers the cells
+// x = 8 qi + 2 t + ((y & 1) ^ c), t < 4.
 // Horizontal neighbours come from the adjacent lane by shuffle, vertical ones
 // from the warp's own registers except across warp boundaries, where each
 // warp publishes its first and last row of the colour it just relaxed in
@@ -31,7 +33,7 @@ constexpr int kRRThreads = 512;
 constexpr int kRRWarps = kRRThreads / 32;
 
 // Shared floats: edge rows [2 colours][16 warps][2 sides], inbox
-// [2 parities][2 sides][2 colours][HK rows], r32 planes [2 colours][R rows],
+// [2 parities][2 sides][2 colours][HK rows], -r32 planes [2 colours][R rows],
 // each row KS = 128 NQ slots.
 __host__ __device__ inline size_t rr_floats(int K, int NQ, int R)
 {
