@@ -127,6 +127,30 @@ def test_stream_sweeps_match_launch_schedule(ctx, n, m, ld):
     assert err < 1e-5, err
 
 
+@pytest.mark.parametrize("n,m", [(8, 64), (16, 40), (40, 300), (64, 33), (136, 257), (200, 100), (256, 512),
+                                 (392, 150), (448, 448), (504, 260), (512, 129), (512, 700)])
+def test_register_resident_cluster_shapes(ctx, n, m):
+    """The register-resident cluster form over its range of shapes (widths a
+    multiple of 8 up to 512: one or two quads per lane, idle lanes, 8- and
+    16-CTA clusters, 2 to 4 rows per warp, 4 or 2 sweeps per exchange, bands
+    shorter than the halo) runs the launch schedule's iteration: after 37
+    mixed-precision sweeps with the same omega the iterates agree to FP32
+    rounding."""
+    import poisson_caustic_design_gb300 as pcd
+
+    b = pcd.inputs.poisson_rhs(n, 12, "binary" if n % 16 else "gaussian", m=m)
+    out = {}
+    for sched in (1, 3):
+        phi = np.zeros_like(b)
+        st = ctx.solve(b, phi, pcd.SolveOptions(stop=pcd.STOP_REL_RESIDUAL, tol=1e-14, max_iterations=37,
+                                                precision=pcd.PREC_MIXED, omega=1.85, schedule=sched))
+        assert st["sweeps"] == 37 and st["schedule_used"] == sched, st
+        out[sched] = phi
+    assert np.isfinite(out[3]).all()
+    err = np.abs(out[3] - out[1]).max() / np.abs(out[1]).max()
+    assert err < 1e-5, err
+
+
 def test_stream_two_sweep_pass_stops_at_max_iterations(ctx):
     """A two-sweep pass launched with one sweep left before max_iterations
     (chunks of 4 sweeps, 37 sweeps) runs a single sweep: the sweep count and
