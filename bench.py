@@ -220,8 +220,10 @@ def run_reference(args, rank, world, pg):
 
 
 def stream_section(ctx, stream, peak):
-    """HBM-bound sweep roofline on 4096^2, 256 sweeps per solve: FP32 stream
-    sweeps (12 B algorithmic per cell-sweep), FP64 in-place stripes (24 B)."""
+    """Sweep rates on 4096^2, 256 sweeps per solve: FP32 stream passes and
+    FP32 register-resident tile passes (12 B algorithmic per cell-sweep; the
+    tile passes move about a quarter of that per sweep, four sweeps per pass),
+    FP64 in-place stripes (24 B)."""
     import torch
 
     import poisson_caustic_design_gb300 as pcd
@@ -231,6 +233,7 @@ def stream_section(ctx, stream, peak):
     p4 = torch.zeros_like(b4)
     out = {}
     for prec, bpc, nm, sch in ((pcd.PREC_MIXED, 12, "fp32_sweeps", pcd.SCHED_STREAM),
+                               (pcd.PREC_MIXED, 12, "fp32_tiles", pcd.SCHED_TILES),
                                (pcd.PREC_FP64, 24, "fp64_sweeps", pcd.SCHED_STRIPES)):
         o4 = pcd.SolveOptions(stop=pcd.STOP_REL_RESIDUAL, tol=0.0, max_iterations=256, omega=-1.0, precision=prec,
                               warm_start=0, schedule=sch, refine_every=256)

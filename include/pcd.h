@@ -92,7 +92,8 @@ typedef enum {
 } pcd_warm_start;
 
 typedef enum {
-    PCD_SCHED_AUTO = 0,        /* cluster, else persistent, else launches, as the grid allows */
+    PCD_SCHED_AUTO = 0,        /* cluster, else persistent, else tiles / stream / stripes, else
+                                  launches, as the grid allows */
     PCD_SCHED_LAUNCHES = 1,    /* one kernel per half sweep, CUDA-graph chunks (any grid) */
     PCD_SCHED_PERSISTENT = 2,  /* one cooperative launch per solve, bands in shared memory
                                   (no NaN cells, band fits on chip) */
@@ -103,11 +104,20 @@ typedef enum {
                                   sweep (row stripes walked top-down, in place), CUDA-graph
                                   chunks; AUTO picks it for FP64 sweeps when the on-chip
                                   schedules do not fit */
-    PCD_SCHED_STREAM = 5       /* mixed precision, grids in HBM without NaN cells, ld a multiple
-                                  of 4, W <= 4096: one pass per sweep from one FP32 correction
-                                  buffer into another (row window in registers, stripe edges
-                                  recomputed, no boundary pass); AUTO picks it for FP32 sweeps
-                                  when the on-chip schedules do not fit */
+    PCD_SCHED_STREAM = 5,      /* mixed precision, grids in HBM without NaN cells, ld a multiple
+                                  of 4, W <= 4096: passes of one or two sweeps from one FP32
+                                  correction buffer into another (row window in registers,
+                                  stripe edges recomputed, no boundary pass); AUTO picks it for
+                                  FP32 sweeps when neither the on-chip schedules nor the tile
+                                  passes apply */
+    PCD_SCHED_TILES = 6        /* mixed precision, grids in HBM without NaN cells, width a multiple
+                                  of 8, ld of 4: passes of up to 4 FP32 sweeps from one correction
+                                  buffer into another, each tile of the grid held in registers
+                                  for the whole pass (halo recomputed); check_every = sweeps per
+                                  pass, i.e. between stop tests (1..4, 0 = 4), so the max |delta|
+                                  stop may come up to 3 sweeps after the first passing sweep;
+                                  AUTO picks it for FP32 sweeps when the on-chip schedules do not
+                                  fit */
 } pcd_schedule;
 
 typedef struct {

@@ -35,6 +35,7 @@ SCHED_PERSISTENT = 2
 SCHED_CLUSTER = 3
 SCHED_STRIPES = 4
 SCHED_STREAM = 5
+SCHED_TILES = 6
 WARM_ZERO = 0
 WARM_GIVEN = 1
 WARM_LEARNED = 2

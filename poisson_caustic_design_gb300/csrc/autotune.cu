@@ -60,9 +60,10 @@ std::vector<TunedSolve> solve_candidates(const pcd_solve_opts &o)
         // cluster (when the grid fits): residual-estimate spacing and cycle drop
         for (int ce : {8, 16, 32, 64}) add(ce, 3e-2, 0, PCD_SCHED_AUTO);
         add(32, 1e-1, 0, PCD_SCHED_AUTO);
-        // grids beyond one cluster: the persistent and stream schedules with
-        // the FP32 sweeps between FP64 refreshes
+        // grids beyond one cluster: the persistent, tile and stream schedules
+        // with the FP32 sweeps between FP64 refreshes
         add(32, 0.0, 0, PCD_SCHED_PERSISTENT);
+        for (int re : {128, 512}) add(4, 0.0, re, PCD_SCHED_TILES);
         for (int re : {128, 512}) add(0, 0.0, re, PCD_SCHED_STREAM);
     } else if (o.precision == PCD_PREC_MIXED) {
         for (int re : {32, 64, 128}) add(0, 0.0, re, PCD_SCHED_AUTO);

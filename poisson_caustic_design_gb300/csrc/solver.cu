@@ -92,25 +92,6 @@ __device__ __forceinline__ T omega_over_cnt(const SolveArgs &a, int cnt)
     return (T)(cnt == 4 ? a.w32[4] : cnt == 3 ? a.w32[3] : cnt == 2 ? a.w32[2] : cnt == 1 ? a.w32[1] : a.w32[0]);
 }
 
-// End-of-sweep bookkeeping, run by the last block of the black half sweep
-// (n sweeps done by a kernel that runs several).
-__device__ void end_of_sweep(Ctl *ctl, const SolveArgs &a, int n = 1)
-{
-    volatile Ctl *c = ctl;
-    unsigned long long bits = atomicExch(&ctl->maxbits, 0ull);
-    double mx = __longlong_as_double((long long)bits);
-    c->last_max = mx;
-    int s = c->sweeps + n;
-    c->sweeps = s;
-    if (a.stop == PCD_STOP_MAX_UPDATE && mx < a.tol) {
-        c->converged = 1;
-        c->halt = 1;
-    }
-    if (s >= a.max_iter) c->halt = 1;
-    c->blocks_done = 0;
-    __threadfence();
-}
-
 // One half sweep over the cells of `color`: delta = omega/cnt*(sum - cnt*v - b)
 // (solver.cpp:47), phi += delta.  TRACK keeps the sweep's max |delta|.
 template <typename T, bool MASKED, bool TRACK>
@@ -452,6 +433,8 @@ struct StreamPlan {
     size_t smem = 0;
     int two = 0;          // two sweeps per pass (k_sweep2_tma) available
     size_t smem2 = 0;
+    TilePlan tile;        // register-resident tile passes (schedule TILES)
+    int tile_sweeps = 0;  // sweeps per tile pass (between stop tests)
 };
 
 int stream_plan(int dev, int W, int H, int ld, bool allow_tma, StreamPlan *p)
@@ -679,6 +662,21 @@ int enqueue_chunk(SolverWorkspace &ws, const double *b, double *phi, const Solve
         }
         sweeps = 0;
     }
+    if (!MASKED && sched == PCD_SCHED_TILES) {
+        // as the stream passes: pass k reads buffer k&1 and writes the other
+        int k = 0;
+        for (int done = 0; done < sweeps; k++) {
+            const float *ein = (k & 1) ? ws.e32b : ws.e32;
+            float *eout = (k & 1) ? ws.e32 : ws.e32b;
+            const int nsw = std::min(sp.tile_sweeps, sweeps - done);
+            PCD_TRY(launch_tile(sp.tile, ein, eout, ws.r32, ws.ctl, a, nsw, (k & 1) ? 0 : 1, track, s));
+            done += nsw;
+            n++;
+        }
+        k_stream_settle<<<rblocks, kThreads, 0, s>>>(ws.e32, ws.e32b, ws.ctl, a);
+        n++;
+        sweeps = 0;
+    }
     if (!MASKED && sched == PCD_SCHED_STREAM) {
         // launch k reads buffer k&1 and writes the other (two sweeps per
         // launch where the plan allows, a single sweep for an odd rest); the
@@ -738,7 +736,8 @@ int get_chunk_graph(SolverWorkspace &ws, const double *b, double *phi, const Sol
                     const StreamPlan &sp)
 {
     std::vector<long long> key = {(long long)(uintptr_t)b, (long long)(uintptr_t)phi, a.W, a.H, a.ld, a.stop,
-                                  a.max_iter, precision, masked, sweeps, sched, sp.G, sp.T, sp.R, sp.tma, sp.two};
+                                  a.max_iter, precision, masked, sweeps, sched, sp.G, sp.T, sp.R, sp.tma, sp.two,
+                                  sp.tile.K, sp.tile.L, sp.tile.NQ, sp.tile_sweeps};
     long long tb, ob;
     std::memcpy(&tb, &a.tol, 8);
     std::memcpy(&ob, &a.omega, 8);
@@ -1073,17 +1072,29 @@ int solve_device(SolverWorkspace &ws, const double *b, double *phi, int W, int H
         PCD_LAUNCHED(1);
     }
 
-    // HBM grids without NaN cells: ping-pong stream sweeps (FP32), else fused
-    // in-place stripe sweeps (grids with at least 3 rows)
+    // HBM grids without NaN cells: ping-pong tile passes or stream sweeps
+    // (FP32), else fused in-place stripe sweeps (grids with at least 3 rows)
     int sched = PCD_SCHED_LAUNCHES;
     StreamPlan sp;
-    if (!masked && precision == PCD_PREC_MIXED &&
-        (o.schedule == PCD_SCHED_AUTO || o.schedule == PCD_SCHED_STREAM || o.schedule == PCD_SCHED_PERSISTENT ||
-         o.schedule == PCD_SCHED_CLUSTER) &&
-        stream_plan(ws.dev, W, H, ld, true, &sp) == PCD_OK)
+    if (!masked && precision == PCD_PREC_MIXED && o.schedule != PCD_SCHED_STREAM &&
+        o.schedule != PCD_SCHED_LAUNCHES && o.schedule != PCD_SCHED_STRIPES) {
+        // register-resident tile passes (4096^2 FP32 sweep: 26 us against the
+        // stream pass's 40 us); check_every: sweeps per pass (stop tests
+        // after every pass), 4 at most
+        sp.tile_sweeps = o.check_every > 0 ? std::min(o.check_every, 4) : 4;
+        if (tile_plan(ws.dev, W, H, ld, sp.tile_sweeps <= 2 ? 2 : 4, &sp.tile) == PCD_OK) sched = PCD_SCHED_TILES;
+    }
+    if (sched == PCD_SCHED_TILES) {
+        // chosen above
+    } else if (!masked && precision == PCD_PREC_MIXED &&
+               (o.schedule == PCD_SCHED_AUTO || o.schedule == PCD_SCHED_STREAM ||
+                o.schedule == PCD_SCHED_PERSISTENT || o.schedule == PCD_SCHED_CLUSTER ||
+                o.schedule == PCD_SCHED_TILES) &&
+               stream_plan(ws.dev, W, H, ld, true, &sp) == PCD_OK) {
         sched = PCD_SCHED_STREAM;
-    else if (!masked && H >= 3 && W <= 2 * kRowCellsMax * kStripeThreads && o.schedule != PCD_SCHED_LAUNCHES)
+    } else if (!masked && H >= 3 && W <= 2 * kRowCellsMax * kStripeThreads && o.schedule != PCD_SCHED_LAUNCHES) {
         sched = PCD_SCHED_STRIPES;
+    }
     const bool stripes = sched == PCD_SCHED_STRIPES;
     if (stripes && ws.stripe_resident == 0) {
         int sms = 0, bps = 0;

@@ -43,6 +43,25 @@ struct SolveArgs {
     float w32[5];    // the same in FP32 ((float)omega / cnt)
 };
 
+// End-of-sweep bookkeeping, run by the last block of the black half sweep
+// (n sweeps done by a kernel that runs several).
+__device__ __forceinline__ void end_of_sweep(Ctl *ctl, const SolveArgs &a, int n = 1)
+{
+    volatile Ctl *c = ctl;
+    unsigned long long bits = atomicExch(&ctl->maxbits, 0ull);
+    double mx = __longlong_as_double((long long)bits);
+    c->last_max = mx;
+    int s = c->sweeps + n;
+    c->sweeps = s;
+    if (a.stop == PCD_STOP_MAX_UPDATE && mx < a.tol) {
+        c->converged = 1;
+        c->halt = 1;
+    }
+    if (s >= a.max_iter) c->halt = 1;
+    c->blocks_done = 0;
+    __threadfence();
+}
+
 // omega > 0: used as given; omega == 0: the reference's 2/(1+pi/width)
 // (solver.cpp:71); omega < 0: 2/(1+sin t) with cos t = (1+cos(pi/n))/2,
 // n = max(width, height), the optimum for the Neumann operator (its slowest

@@ -471,6 +471,24 @@ __global__ void __launch_bounds__(kClusterThreads, 1) k_sor_cluster_tb(ClusterAr
 }
 
 #include "sor_cluster_rr.cuh"
+#include "sor_tile_rr.cuh"
+
+template <int K, bool TRACK>
+const void *tile_kernel_k(int L, int NQ)
+{
+    if (L == 3 && NQ == 2) return (const void *)k_sor_tile_rr<K, 3, 2, TRACK>;
+    if (L == 4 && NQ == 1) return (const void *)k_sor_tile_rr<K, 4, 1, TRACK>;
+    return nullptr;
+}
+
+// The tile pass for K sweeps, L rows per warp and NQ quads per lane (nullptr
+// outside the compiled set).
+const void *tile_kernel(int K, int L, int NQ, bool track)
+{
+    if (K == 4) return track ? tile_kernel_k<4, true>(L, NQ) : tile_kernel_k<4, false>(L, NQ);
+    if (K == 2) return track ? tile_kernel_k<2, true>(L, NQ) : tile_kernel_k<2, false>(L, NQ);
+    return nullptr;
+}
 
 }  // namespace
 
@@ -574,6 +592,70 @@ int cluster_plan(int dev, int W, int H, int max_depth, ClusterPlan *plan)
         }
     }
     return PCD_BAD_ARG;
+}
+
+int tile_plan(int dev, int W, int H, int ld, int depth, TilePlan *plan)
+{
+    if (W < 8 || H < 1 || W % 8 != 0 || ld % 4 != 0) return PCD_BAD_ARG;
+    if (depth != 0 && depth != 2 && depth != 4) return PCD_BAD_ARG;
+    const int K = depth ? depth : 4;
+    int sms = 0, max_smem = 0;
+    PCD_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    PCD_CUDA(cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    const int WQ = W / 8;
+    TilePlan best{};
+    long best_cost = 0;
+    // tiles of 16 L rows and 256 NQ columns; a tile costs about L NQ quad
+    // updates per thread and half sweep whatever its interior
+    const int forms[2][2] = {{3, 2}, {4, 1}};
+    for (const auto &f : forms) {
+        const int L = f[0], NQ = f[1];
+        const int N = kRRWarps * L - 4 * K;
+        if (N < 1) continue;
+        const int ncol = ceil_div(WQ, 32 * NQ - 2), nrow = ceil_div(H, N);
+        const long cost = (long)ncol * nrow * L * NQ;
+        if (best.K && cost >= best_cost) continue;
+        const size_t smem = tile_floats(L, NQ) * sizeof(float);
+        if (smem + 2048 > (size_t)max_smem) continue;
+        int bps = 1;
+        for (int tr = 0; tr < 2; tr++) {
+            const void *fn = tile_kernel(K, L, NQ, tr != 0);
+            if (!fn) {
+                bps = 0;
+                break;
+            }
+            int b = 0;
+            PCD_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            PCD_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, fn, kRRThreads, smem));
+            bps = std::min(bps, b);
+        }
+        if (bps < 1) continue;
+        best.K = K;
+        best.L = L;
+        best.NQ = NQ;
+        best.ncol = ncol;
+        best.nrow = nrow;
+        best.grid = (int)std::min<long>((long)ncol * nrow, (long)sms * bps);
+        best.smem = smem;
+        best_cost = cost;
+    }
+    if (!best.K) return PCD_BAD_ARG;
+    *plan = best;
+    return PCD_OK;
+}
+
+int launch_tile(const TilePlan &p, const float *ein, float *eout, const float *r32, Ctl *ctl, const SolveArgs &a,
+                int nsw, int out_idx, bool track, cudaStream_t s)
+{
+    const void *fn = tile_kernel(p.K, p.L, p.NQ, track);
+    if (!fn || nsw < 1 || nsw > p.K) {
+        set_error("tile SOR: no kernel for this plan");
+        return PCD_BAD_ARG;
+    }
+    using Fn = void (*)(const float *, float *, const float *, Ctl *, SolveArgs, int, int, int, int);
+    reinterpret_cast<Fn>(const_cast<void *>(fn))<<<p.grid, kRRThreads, p.smem, s>>>(ein, eout, r32, ctl, a, p.ncol,
+                                                                                    p.nrow, nsw, out_idx);
+    return PCD_OK;
 }
 
 int launch_cluster(ClusterArgs &a, const ClusterPlan &p, cudaStream_t s)

@@ -42,4 +42,22 @@ struct ClusterPlan {
 int cluster_plan(int dev, int W, int H, int max_depth, ClusterPlan *plan);
 int launch_cluster(ClusterArgs &a, const ClusterPlan &p, cudaStream_t s);
 
+// Register-resident tile passes for grids in HBM (FP32 correction sweeps,
+// ping-pong buffers): K sweeps per pass, tiles of 16 L rows and 256 NQ
+// columns (halo included), ncol x nrow tiles on `grid` persistent CTAs.
+struct TilePlan {
+    int K = 0, L = 0, NQ = 0;
+    int ncol = 0, nrow = 0, grid = 0;
+    size_t smem = 0;
+};
+
+// The plan for a W x H grid with leading dimension ld (W a multiple of 8, ld
+// of 4); depth = sweeps per pass (2 or 4; 0: 4).  PCD_BAD_ARG when no form
+// applies.
+int tile_plan(int dev, int W, int H, int ld, int depth, TilePlan *plan);
+// One pass of nsw <= K sweeps from ein into eout (fewer at the sweep cap);
+// track: the pass reports the largest |update| of its last sweep.
+int launch_tile(const TilePlan &p, const float *ein, float *eout, const float *r32, Ctl *ctl, const SolveArgs &a,
+                int nsw, int out_idx, bool track, cudaStream_t s);
+
 }  // namespace pcd

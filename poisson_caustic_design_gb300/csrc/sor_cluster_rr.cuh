@@ -63,6 +63,12 @@ __device__ __forceinline__ float4 quad_ghost_q(int q, const float4 &v, const flo
     return make_float4(nA.x, nA.y, nB.x, nB.y);
 }
 
+// Largest |nv - v| over the quad (a NaN change does not raise it).
+__device__ __forceinline__ float quad_max_change(const float4 &v, const float4 &nv)
+{
+    return fmaxf(fmaxf(fabsf(nv.x - v.x), fabsf(nv.y - v.y)), fmaxf(fabsf(nv.z - v.z), fabsf(nv.w - v.w)));
+}
+
 // Sum of squares of r32 - L v over the quad (ghost neighbours as above; nrh
 // is -r32).
 __device__ __forceinline__ float quad_ghost_res2(int q, const float4 &v, const float4 &nrh, const float4 &u,
@@ -85,6 +91,7 @@ struct RRState {
     float4 e[2][L][NQ];      // both colours of the warp's rows
     float2 waa[NQ], wla[NQ], war[NQ];  // weight pairs: (wa, wa), (wl, wa), (wa, wr)
     bool act[NQ], eL[NQ], eR[NQ];
+    bool own[NQ];            // tile passes: quad in the tile's interior columns
     float w4, w3, w2, w1;
     int lane, w, H, ybase, R;
     unsigned edge_s, r_s;    // shared addresses of slot 4 * lane of edge row 0 / -r32 row 0
@@ -118,9 +125,10 @@ struct RRState {
     }
 
     // Half sweep of colour CC over plane rows [lo, hi); P = parity of the
-    // grid row of the warp's first row.
-    template <int CC, int P>
-    __device__ __forceinline__ void half(int lo, int hi)
+    // grid row of the warp's first row.  TR: mx takes the largest |update| of
+    // the cells of plane rows [olo, ohi) in quads marked own.
+    template <int CC, int P, bool TR = false>
+    __device__ __forceinline__ void half(int lo, int hi, float *mx = nullptr, int olo = 0, int ohi = 0)
     {
         constexpr int OC = 1 - CC;
         float4 eu[NQ], ed[NQ];
@@ -161,7 +169,10 @@ struct RRState {
                     if (q ? eL[i] : eR[i]) ex = q ? v.x : v.w;
                     const float4 u = j > 0 ? e[OC][j > 0 ? j - 1 : 0][i] : eu[i];
                     const float4 d = j + 1 < L ? e[OC][j + 1 < L ? j + 1 : j][i] : ed[i];
-                    e[CC][j][i] = quad_ghost_q(q, v, rh, u, d, e[OC][j][i], ex, q ? wla[i] : waa[i], q ? waa[i] : war[i]);
+                    const float4 nv =
+                        quad_ghost_q(q, v, rh, u, d, e[OC][j][i], ex, q ? wla[i] : waa[i], q ? waa[i] : war[i]);
+                    if (TR && own[i] && lr0 + j >= olo && lr0 + j < ohi) *mx = fmaxf(*mx, quad_max_change(v, nv));
+                    e[CC][j][i] = nv;
                 }
             }
         } else {
@@ -191,7 +202,9 @@ struct RRState {
                     const float a = !on || !act[i] ? 0.f : brd ? (two ? w3 : w2) : w4;
                     const float we = !on ? 0.f : edge ? (brd ? (two ? w2 : w1) : w3) : a;
                     const float2 wA = make_float2(q ? we : a, a), wB = make_float2(a, q ? a : we);
-                    e[CC][j][i] = quad_ghost_q(q, v, rh, u, d, e[OC][j][i], ex, wA, wB);
+                    const float4 nv = quad_ghost_q(q, v, rh, u, d, e[OC][j][i], ex, wA, wB);
+                    if (TR && on && own[i] && lr >= olo && lr < ohi) *mx = fmaxf(*mx, quad_max_change(v, nv));
+                    e[CC][j][i] = nv;
                 }
             }
         }

@@ -20,12 +20,12 @@ import numpy as np
 
 from . import _lib
 from ._lib import (PREC_FP64, PREC_MIXED, SCHED_AUTO, SCHED_CLUSTER, SCHED_LAUNCHES, SCHED_PERSISTENT, SCHED_STREAM,
-                   SCHED_STRIPES, STOP_MAX_UPDATE,
+                   SCHED_STRIPES, SCHED_TILES, STOP_MAX_UPDATE,
                    STOP_REL_RESIDUAL, check)
 
 __all__ = ["poisson_solver", "batch_solve", "solver_progress", "Context", "SolveOptions", "PREC_FP64", "PREC_MIXED",
            "STOP_MAX_UPDATE", "STOP_REL_RESIDUAL", "SCHED_AUTO", "SCHED_LAUNCHES", "SCHED_PERSISTENT",
-           "SCHED_CLUSTER", "SCHED_STRIPES", "SCHED_STREAM"]
+           "SCHED_CLUSTER", "SCHED_STRIPES", "SCHED_STREAM", "SCHED_TILES"]
 
 # solver.h:10 declares `extern double solver_progress`; the reference never
 # updates it (solver.cpp:9,63-68), so neither does this mirror.

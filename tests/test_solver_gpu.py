@@ -16,7 +16,7 @@ from conftest import load_golden, solver_case_names
 pytestmark = pytest.mark.gpu
 
 RTOL_PLAIN = 1e-5
-SCHEDS = [1, 2]  # launch-per-half-sweep, persistent (4 = fused stripes, 3 = cluster, 5 = stream)
+SCHEDS = [1, 2]  # launch-per-half-sweep, persistent (4 = fused stripes, 3 = cluster, 5 = stream, 6 = tiles)
 
 
 def _rel_mod_const(x, ref):
@@ -47,7 +47,7 @@ def test_legacy_poisson_solver_matches_reference(name):
     assert e2 < RTOL_PLAIN, (name, e2, emax)
 
 
-@pytest.mark.parametrize("sched", SCHEDS + [5])
+@pytest.mark.parametrize("sched", SCHEDS + [5, 6])
 @pytest.mark.parametrize("prec", [0, 1])
 def test_stats_and_reference_stop_semantics(ctx, sched, prec):
     import poisson_caustic_design_gb300 as pcd
@@ -81,20 +81,21 @@ def test_persistent_and_launch_schedules_agree(ctx, n, m):
         assert np.abs(out[0] - o).max() <= 1e-9 * np.abs(out[0]).max()
 
 
-@pytest.mark.parametrize("prec", [0, 1])
-def test_stripes_on_grid_beyond_chip(ctx, prec):
-    """A grid too large for the on-chip schedules runs the fused stripe
-    sweeps and reaches the exact solve."""
+@pytest.mark.parametrize("n,prec,sched", [(2048, 0, 4), (2048, 1, 6), (2044, 1, 5)])
+def test_stripes_on_grid_beyond_chip(ctx, n, prec, sched):
+    """A grid too large for the on-chip schedules reaches the exact solve on
+    the HBM schedules that AUTO picks: 1800/148 rows x 2048 x 16 B exceed
+    shared memory, so FP64 sweeps run the in-place stripes and FP32
+    correction sweeps the register-resident tile passes (width a multiple of
+    8) or the ping-pong stream passes (2044 columns)."""
     import oracle
     import poisson_caustic_design_gb300 as pcd
 
-    b = pcd.inputs.poisson_rhs(2048, 6, "gaussian", m=1800)
+    b = pcd.inputs.poisson_rhs(n, 6, "gaussian", m=1800)
     phi = np.zeros_like(b)
     st = ctx.solve(b, phi, pcd.SolveOptions(stop=pcd.STOP_REL_RESIDUAL, tol=1e-8, max_iterations=100000,
                                             omega=-1.0, precision=prec))
-    # 1800/148 rows x 2048 x 16 B exceed shared memory: FP64 sweeps run the
-    # in-place stripes, FP32 correction sweeps the ping-pong stream kernel
-    assert st["converged"] and st["schedule_used"] == (5 if prec else 4)
+    assert st["converged"] and st["schedule_used"] == sched, st
     assert _rel_mod_const(phi, oracle.dct_solve(b))[0] < 1e-6
 
 
@@ -227,6 +228,72 @@ def test_stream_sweeps_reach_exact_solve(ctx):
     st = ctx.solve(b, phi, pcd.SolveOptions(stop=pcd.STOP_REL_RESIDUAL, tol=1e-8, max_iterations=200000,
                                             omega=-1.0, precision=pcd.PREC_MIXED, schedule=5))
     assert st["converged"] and st["schedule_used"] == 5
+    assert _rel_mod_const(phi, oracle.dct_solve(b))[0] < 1e-6
+
+
+@pytest.mark.parametrize("n,m,ld,per_pass", [(4096, 300, 4096, 4), (2048, 1800, 2048, 2), (1000, 37, 1000, 3),
+                                             (1024, 64, 1032, 1), (496, 260, 496, 4), (240, 7, 240, 4),
+                                             (8, 40, 8, 4), (248, 100, 252, 2), (512, 512, 512, 4)])
+def test_tile_passes_match_launch_schedule(ctx, n, m, ld, per_pass):
+    """The register-resident tile passes (up to 4 sweeps per pass from one
+    FP32 buffer into the other, every tile's halo rows and columns
+    recomputed) run the same red-black iteration as the launch-per-half-sweep
+    kernels: after the same odd number of mixed-precision sweeps (the last
+    pass of each chunk shorter) the iterates agree to FP32 rounding.  Covers
+    both tile forms (16 x 512 and 4 x 256 cells per warp: 496 columns take the
+    first, the others the second), 4 and 2 sweeps per pass (check_every 1 to
+    4), padded rows, grids shorter than one tile and one tile column."""
+    import torch
+
+    import poisson_caustic_design_gb300 as pcd
+
+    b = pcd.inputs.poisson_rhs(n, 10, "binary" if m % 2 else "gaussian", m=m)
+    bd = torch.zeros((m, ld), dtype=torch.float64, device="cuda")[:, :n]
+    bd.copy_(torch.from_numpy(b))
+    out = {}
+    for sched in (1, 6):
+        pd = torch.zeros((m, ld), dtype=torch.float64, device="cuda")[:, :n]
+        st = ctx.solve_device(bd, pd, pcd.SolveOptions(stop=pcd.STOP_REL_RESIDUAL, tol=0.0, max_iterations=37,
+                                                       precision=pcd.PREC_MIXED, omega=-1.0, schedule=sched,
+                                                       check_every=per_pass if sched == 6 else 0, refine_every=16))
+        assert st["sweeps"] == 37 and st["schedule_used"] == sched, st
+        out[sched] = pd.cpu().numpy()
+    assert np.isfinite(out[6]).all()
+    err = np.abs(out[6] - out[1]).max() / np.abs(out[1]).max()
+    assert err < 1e-5, err
+
+
+def test_tile_max_update_stop_matches_plain(ctx):
+    """The reference's stop rule on the tile schedule, where each pass tracks
+    the largest update of its last sweep: the mixed solve stops within a few
+    sweeps of the plain FP64 one and lands as close to the exact solution."""
+    import oracle
+    import poisson_caustic_design_gb300 as pcd
+
+    b = pcd.inputs.poisson_rhs(1024, 6, "gaussian", m=256)
+    exact = oracle.dct_solve(b)
+    res = {}
+    for name, prec, sched in (("plain", pcd.PREC_FP64, 1), ("mixed", pcd.PREC_MIXED, 6)):
+        phi = np.zeros_like(b)
+        st = ctx.solve(b, phi, pcd.SolveOptions(stop=pcd.STOP_MAX_UPDATE, tol=1e-7, max_iterations=200000,
+                                                precision=prec, omega=-1.0, schedule=sched))
+        assert st["converged"] and st["schedule_used"] == sched
+        res[name] = (st["sweeps"], _rel_mod_const(phi, exact)[0])
+    (sp, ep), (sm, em) = res["plain"], res["mixed"]
+    assert abs(sm - sp) <= 0.03 * sp, (sp, sm)
+    assert em <= 1.5 * ep + 1e-9, (ep, em)
+
+
+def test_tile_passes_reach_exact_solve(ctx):
+    """4096 columns (18 tile columns) to 1e-8 against the DCT solve."""
+    import oracle
+    import poisson_caustic_design_gb300 as pcd
+
+    b = pcd.inputs.poisson_rhs(4096, 12, "gaussian", m=512)
+    phi = np.zeros_like(b)
+    st = ctx.solve(b, phi, pcd.SolveOptions(stop=pcd.STOP_REL_RESIDUAL, tol=1e-8, max_iterations=200000,
+                                            omega=-1.0, precision=pcd.PREC_MIXED, schedule=6))
+    assert st["converged"] and st["schedule_used"] == 6
     assert _rel_mod_const(phi, oracle.dct_solve(b))[0] < 1e-6
 
 
