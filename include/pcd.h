@@ -92,8 +92,9 @@ typedef enum {
 } pcd_warm_start;
 
 typedef enum {
-    PCD_SCHED_AUTO = 0,        /* cluster, else persistent, else tiles / stream / stripes, else
-                                  launches, as the grid allows */
+    PCD_SCHED_AUTO = 0,        /* FP32 sweeps: cluster, else tiles (grids of at least 64 x 64
+                                  cells), else persistent, else stream; FP64: persistent, else
+                                  stripes; else launches, as the grid allows */
     PCD_SCHED_LAUNCHES = 1,    /* one kernel per half sweep, CUDA-graph chunks (any grid) */
     PCD_SCHED_PERSISTENT = 2,  /* one cooperative launch per solve, bands in shared memory
                                   (no NaN cells, band fits on chip) */
@@ -116,8 +117,8 @@ typedef enum {
                                   for the whole pass (halo recomputed); check_every = sweeps per
                                   pass, i.e. between stop tests (1..4, 0 = 4), so the max |delta|
                                   stop may come up to 3 sweeps after the first passing sweep;
-                                  AUTO picks it for FP32 sweeps when the on-chip schedules do not
-                                  fit */
+                                  AUTO picks it for FP32 sweeps when the cluster schedule does
+                                  not apply */
 } pcd_schedule;
 
 typedef struct {

@@ -67,6 +67,7 @@ std::vector<TunedSolve> solve_candidates(const pcd_solve_opts &o)
         for (int re : {128, 512}) add(0, 0.0, re, PCD_SCHED_STREAM);
     } else if (o.precision == PCD_PREC_MIXED) {
         for (int re : {32, 64, 128}) add(0, 0.0, re, PCD_SCHED_AUTO);
+        add(0, 0.0, 0, PCD_SCHED_PERSISTENT);
     } else {
         for (int ce : {8, 32}) add(ce, 0.0, 0, PCD_SCHED_AUTO);
         add(32, 0.0, 0, PCD_SCHED_STRIPES);

@@ -284,6 +284,27 @@ def test_tile_max_update_stop_matches_plain(ctx):
     assert em <= 1.5 * ep + 1e-9, (ep, em)
 
 
+@pytest.mark.parametrize("n,stop", [(64, 0), (256, 0), (768, 1)])
+def test_auto_routes_fp32_sweeps_to_tiles(ctx, n, stop):
+    """AUTO runs FP32 sweeps that the cluster schedule does not take (the
+    max-update stop, or more than 512 columns) on the tile passes, and the
+    persistent schedule only on request; both reach the same solution."""
+    import oracle
+    import poisson_caustic_design_gb300 as pcd
+
+    b = pcd.inputs.poisson_rhs(n, 3, "gaussian")
+    exact = oracle.dct_solve(b)
+    tol = 1e-8 if stop == 0 else 1e-7
+    out = {}
+    for sched, used in ((0, 6), (2, 2)):
+        phi = np.zeros_like(b)
+        st = ctx.solve(b, phi, pcd.SolveOptions(stop=stop, tol=tol, max_iterations=200000, omega=-1.0,
+                                                precision=pcd.PREC_MIXED, schedule=sched))
+        assert st["converged"] and st["schedule_used"] == used, st
+        out[sched] = _rel_mod_const(phi, exact)[0]
+    assert out[0] <= 1.5 * out[2] + 1e-9, out
+
+
 def test_tile_passes_reach_exact_solve(ctx):
     """4096 columns (18 tile columns) to 1e-8 against the DCT solve."""
     import oracle
