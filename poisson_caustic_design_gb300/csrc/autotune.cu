@@ -217,6 +217,14 @@ int batch_autotuned(pcd_ctx *ctx, const pcd_instance *inst, int count, const pcd
             t.refine_drop = 3e-2;
             cand.push_back(t);
         }
+    if (batch_tiles_apply(inst, count)) {
+        // the batched tile passes (cluster 0 with the default schedule)
+        TunedBatch t;
+        t.cluster = 0;
+        t.check_every = 0;
+        t.refine_drop = 0.0;
+        cand.push_back(t);
+    }
     std::vector<pcd_instance_stats> tmp((size_t)count);
     int best = -1;
     double best_ms = 0.0;

@@ -1189,4 +1189,360 @@ int solve_device(SolverWorkspace &ws, const double *b, double *phi, int W, int H
     return c.converged ? PCD_OK : PCD_NOT_CONVERGED;
 }
 
+
+// ---------------------------------------------------------------------------
+// Batched tile solve: the grids of a batch share one tile pass per launch
+// (k_sor_tile_batch) and one FP64 refresh pair per chunk of passes, each
+// grid with its own control block, so a grid that has converged drops out
+// while the others go on.
+namespace {
+
+// One grid of the batched FP64 refresh: blocks [blk0, blk0 + nblk) of the
+// launch work on it.
+struct RefineJob {
+    const double *b;
+    double *phi;
+    float *e, *eb;       // the correction buffers (eb holds the latest when stream_out is set)
+    float *r32;
+    Ctl *ctl;
+    double *partials;    // 3 per block
+    int W, H, ld;
+    int blk0, nblk;
+};
+
+constexpr int kBatchRefineBlocks = 64;  // per grid at most
+constexpr int kBatchChunkPasses = 16;   // tile passes (of 4 sweeps) between FP64 refreshes
+
+__device__ __forceinline__ int refine_job(const RefineJob *jobs, int njobs, int blk)
+{
+    int lo = 0, hi = njobs - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (__ldg(&jobs[mid].blk0) <= blk) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+__device__ __forceinline__ bool last_block_of(Ctl *ctl, int nblk)
+{
+    __shared__ bool is_last;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        const unsigned t = atomicAdd(&ctl->blocks_done_r, 1u);
+        is_last = (t == (unsigned)nblk - 1u);
+    }
+    __syncthreads();
+    if (is_last) __threadfence();
+    return is_last;
+}
+
+// r = b - L(phi + e) in FP64 per grid (the latest correction buffer), r32 =
+// (float) r, norms and the relative-residual test by each grid's last block.
+__global__ void __launch_bounds__(kThreads)
+    k_batch_refine_residual(const RefineJob *__restrict__ jobs, int njobs, double tol, int with_b)
+{
+    const RefineJob &J = jobs[refine_job(jobs, njobs, blockIdx.x)];
+    Ctl *ctl = J.ctl;
+    if (vol_load(&ctl->done)) return;
+    const float *__restrict__ e = vol_load(&ctl->stream_out) ? J.eb : J.e;
+    const int lb = (int)blockIdx.x - J.blk0, W = J.W, H = J.H, ld = J.ld;
+    const long n = (long)W * H;
+    double v[3] = {0.0, 0.0, 0.0};
+    for (long t = (long)lb * blockDim.x + threadIdx.x; t < n; t += (long)J.nblk * blockDim.x) {
+        const int y = (int)(t / W), x = (int)(t - (long)y * W);
+        const long i = (long)y * ld + x;
+        const double bi = J.b[i];
+        double sum = 0.0, cnt = 0.0;
+        if (x > 0) { cnt += 1.0; sum += J.phi[i - 1] + (double)e[i - 1]; }
+        if (y > 0) { cnt += 1.0; sum += J.phi[i - ld] + (double)e[i - ld]; }
+        if (x < W - 1) { cnt += 1.0; sum += J.phi[i + 1] + (double)e[i + 1]; }
+        if (y < H - 1) { cnt += 1.0; sum += J.phi[i + ld] + (double)e[i + ld]; }
+        const double xi = J.phi[i] + (double)e[i];
+        const double r = bi - (sum - cnt * xi);
+        J.r32[i] = (float)r;
+        if (isnan(bi)) continue;
+        v[0] += r * r;
+        v[1] += bi * bi;
+        v[2] = nan_skip_max(v[2], fabs(r));
+    }
+    block_reduce<3, 4u>(v);
+    if (threadIdx.x == 0) {
+        J.partials[3 * lb] = v[0];
+        J.partials[3 * lb + 1] = v[1];
+        J.partials[3 * lb + 2] = v[2];
+    }
+    if (last_block_of(ctl, J.nblk)) {
+        SolveArgs a{};
+        a.stop = PCD_STOP_REL_RESIDUAL;
+        a.tol = tol;
+        finalize_residual(ctl, J.partials, J.nblk, a, 1, with_b);
+    }
+}
+
+// phi += latest correction, e = 0 per grid; a halted grid is done.
+__global__ void __launch_bounds__(kThreads) k_batch_refine_update(const RefineJob *__restrict__ jobs, int njobs)
+{
+    const RefineJob &J = jobs[refine_job(jobs, njobs, blockIdx.x)];
+    Ctl *ctl = J.ctl;
+    if (vol_load(&ctl->done)) return;
+    const float *el = vol_load(&ctl->stream_out) ? J.eb : J.e;
+    const int lb = (int)blockIdx.x - J.blk0, W = J.W, ld = J.ld;
+    const long n = (long)W * J.H;
+    for (long t = (long)lb * blockDim.x + threadIdx.x; t < n; t += (long)J.nblk * blockDim.x) {
+        const int y = (int)(t / W), x = (int)(t - (long)y * W);
+        const long i = (long)y * ld + x;
+        J.phi[i] += (double)el[i];
+        J.e[i] = 0.0f;
+    }
+    if (last_block_of(ctl, J.nblk)) {
+        if (threadIdx.x == 0) {
+            volatile Ctl *c = ctl;
+            if (c->halt) c->done = 1;
+            c->stream_out = 0;
+            c->blocks_done_r = 0;
+            __threadfence();
+        }
+    }
+}
+
+}  // namespace
+
+int TileBatchWorkspace::reserve(size_t floats, int count)
+{
+    if (floats > arena_floats) {
+        for (auto &kv : graphs) cudaGraphExecDestroy(kv.second);
+        graphs.clear();
+        if (arena) cudaFree(arena);
+        arena = nullptr;
+        arena_floats = 0;
+        PCD_CUDA(cudaMalloc(&arena, floats * sizeof(float)));
+        arena_floats = floats;
+    }
+    if (count > cap) {
+        for (auto &kv : graphs) cudaGraphExecDestroy(kv.second);
+        graphs.clear();
+        if (ctl) cudaFree(ctl);
+        if (ctl_host) cudaFreeHost(ctl_host);
+        if (partials) cudaFree(partials);
+        if (jobs) cudaFree(jobs);
+        if (rjobs) cudaFree(rjobs);
+        ctl = nullptr; ctl_host = nullptr; partials = nullptr; jobs = nullptr; rjobs = nullptr;
+        cap = 0;
+        PCD_CUDA(cudaMalloc(&ctl, sizeof(Ctl) * count));
+        PCD_CUDA(cudaMallocHost(&ctl_host, 2 * sizeof(Ctl) * count));
+        PCD_CUDA(cudaMalloc(&partials, sizeof(double) * 3 * kBatchRefineBlocks * count));
+        PCD_CUDA(cudaMalloc(&jobs, sizeof(TileJob) * count));
+        PCD_CUDA(cudaMalloc(&rjobs, sizeof(RefineJob) * count));
+        cap = count;
+    }
+    if (!t0) {
+        PCD_CUDA(cudaEventCreate(&t0));
+        PCD_CUDA(cudaEventCreate(&t1));
+        PCD_CUDA(cudaEventCreateWithFlags(&ev[0], cudaEventDisableTiming));
+        PCD_CUDA(cudaEventCreateWithFlags(&ev[1], cudaEventDisableTiming));
+        PCD_CUDA(cudaMalloc(&counter, sizeof(unsigned)));
+    }
+    return PCD_OK;
+}
+
+void TileBatchWorkspace::release()
+{
+    for (auto &kv : graphs) cudaGraphExecDestroy(kv.second);
+    graphs.clear();
+    if (arena) cudaFree(arena);
+    if (ctl) cudaFree(ctl);
+    if (ctl_host) cudaFreeHost(ctl_host);
+    if (partials) cudaFree(partials);
+    if (jobs) cudaFree(jobs);
+    if (rjobs) cudaFree(rjobs);
+    if (counter) cudaFree(counter);
+    for (cudaEvent_t *e : {&t0, &t1, &ev[0], &ev[1]})
+        if (*e) cudaEventDestroy(*e);
+    *this = TileBatchWorkspace();
+}
+
+bool batch_tiles_apply(const pcd_instance *inst, int count)
+{
+    if (!inst || count < 1 || count > kTileBatchJobsMax) return false;
+    for (int i = 0; i < count; i++) {
+        const pcd_instance &q = inst[i];
+        if (!q.b || !q.phi || q.width < 8 || q.height < 1 || q.width % 8 != 0 || q.ld < q.width || q.ld % 4 != 0)
+            return false;
+    }
+    return true;
+}
+
+int batch_tiles_solve(TileBatchWorkspace &ws, int dev, const pcd_instance *inst, int count, const pcd_solve_opts &o,
+                      pcd_instance_stats *stats, pcd_batch_stats *bstats, cudaStream_t s)
+{
+    if (!batch_tiles_apply(inst, count)) {
+        set_error("batched tile solve: every grid needs a width that is a multiple of 8 and ld a multiple of 4, "
+                  "and at most " + std::to_string(kTileBatchJobsMax) + " grids");
+        return PCD_BAD_ARG;
+    }
+    if (o.stop != PCD_STOP_REL_RESIDUAL || !(o.tol > 0.0) || o.max_iterations < 1) {
+        set_error("pcd_batch_solve_device: the batch solve takes the relative-residual stop with tol > 0");
+        return PCD_BAD_ARG;
+    }
+    size_t smem = 0;
+    int grid = 0;
+    PCD_TRY(tile_batch_config(dev, count, &smem, &grid));
+    size_t per = 0;
+    for (int i = 0; i < count; i++) per += (size_t)inst[i].height * inst[i].ld;
+    PCD_TRY(ws.reserve(3 * per, count));
+
+    std::vector<TileJob> tj((size_t)count);
+    std::vector<RefineJob> rj((size_t)count);
+    size_t off = 0;
+    int tiles = 0, blocks = 0;
+    for (int i = 0; i < count; i++) {
+        const pcd_instance &q = inst[i];
+        TileJob &t = tj[i];
+        RefineJob &r = rj[i];
+        t.ea = ws.arena + off;
+        t.eb = ws.arena + per + off;
+        t.r32 = ws.arena + 2 * per + off;
+        t.ctl = ws.ctl + i;
+        t.W = q.width;
+        t.H = q.height;
+        t.ld = q.ld;
+        tile_counts(q.width, q.height, &t.ncol, &t.nrow);
+        t.tile0 = tiles;
+        t.max_iter = o.max_iterations;
+        const double om = resolve_omega(o.omega, q.width, q.height);
+        for (int c = 0; c < 5; c++) t.w32[c] = (float)om / (float)c;
+        tiles += t.ncol * t.nrow;
+        r.b = q.b;
+        r.phi = q.phi;
+        r.e = t.ea;
+        r.eb = t.eb;
+        r.r32 = ws.arena + 2 * per + off;
+        r.ctl = t.ctl;
+        r.partials = ws.partials + (size_t)3 * kBatchRefineBlocks * i;
+        r.W = q.width;
+        r.H = q.height;
+        r.ld = q.ld;
+        r.blk0 = blocks;
+        r.nblk = (int)std::min<long>(kBatchRefineBlocks, ((long)q.width * q.height + kThreads - 1) / kThreads);
+        blocks += r.nblk;
+        off += (size_t)q.height * q.ld;
+    }
+    const TileJob *d_jobs = static_cast<const TileJob *>(ws.jobs);
+    const RefineJob *d_rjobs = static_cast<const RefineJob *>(ws.rjobs);
+    const int passes = o.refine_every > 0 ? std::max(1, (o.refine_every + 3) / 4) : kBatchChunkPasses;
+
+    PCD_CUDA(cudaEventRecord(ws.t0, s));
+    PCD_CUDA(cudaMemcpyAsync(ws.jobs, tj.data(), sizeof(TileJob) * count, cudaMemcpyHostToDevice, s));
+    PCD_CUDA(cudaMemcpyAsync(ws.rjobs, rj.data(), sizeof(RefineJob) * count, cudaMemcpyHostToDevice, s));
+    PCD_CUDA(cudaMemsetAsync(ws.ctl, 0, sizeof(Ctl) * count, s));
+    PCD_CUDA(cudaMemsetAsync(ws.counter, 0, sizeof(unsigned), s));
+    PCD_CUDA(cudaMemsetAsync(ws.arena, 0, sizeof(float) * per, s));
+    if (!o.warm_start)
+        for (int i = 0; i < count; i++)
+            PCD_CUDA(cudaMemset2DAsync(inst[i].phi, sizeof(double) * inst[i].ld, 0, sizeof(double) * inst[i].width,
+                                       inst[i].height, s));
+    // first right-hand side, ||b|| and the stop test of the starting phi
+    k_batch_refine_residual<<<blocks, kThreads, 0, s>>>(d_rjobs, count, o.tol, 1);
+    k_batch_refine_update<<<blocks, kThreads, 0, s>>>(d_rjobs, count);
+    PCD_LAUNCHED(2);
+
+    // one CUDA graph per batch signature: the chunk's passes and the refresh
+    std::vector<long long> key = {count, tiles, blocks, passes, grid, (long long)smem,
+                                  (long long)(uintptr_t)ws.jobs, (long long)(uintptr_t)ws.rjobs};
+    {
+        long long tb;
+        std::memcpy(&tb, &o.tol, 8);
+        key.push_back(tb);
+    }
+    cudaGraphExec_t exec = nullptr;
+    auto it = ws.graphs.find(key);
+    if (it != ws.graphs.end()) {
+        exec = it->second;
+    } else {
+        cudaGraph_t g;
+        PCD_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+        int st = PCD_OK;
+        for (int k = 0; k < passes && st == PCD_OK; k++)
+            st = launch_tile_batch(d_jobs, count, tiles, 4, k & 1, grid, smem, ws.counter, s);
+        k_batch_refine_residual<<<blocks, kThreads, 0, s>>>(d_rjobs, count, o.tol, 0);
+        k_batch_refine_update<<<blocks, kThreads, 0, s>>>(d_rjobs, count);
+        cudaError_t ce = cudaStreamEndCapture(s, &g);
+        if (st != PCD_OK) return st;
+        if (ce != cudaSuccess) {
+            set_error(std::string("batched tile graph capture: ") + cudaGetErrorString(ce));
+            return PCD_DEVICE_ERROR;
+        }
+        ce = cudaGraphInstantiate(&exec, g, 0);
+        cudaGraphDestroy(g);
+        if (ce != cudaSuccess) {
+            set_error(std::string("batched tile graph instantiate: ") + cudaGetErrorString(ce));
+            return PCD_DEVICE_ERROR;
+        }
+        if (ws.graphs.size() > 16) {
+            for (auto &kv : ws.graphs) cudaGraphExecDestroy(kv.second);
+            ws.graphs.clear();
+        }
+        ws.graphs[key] = exec;
+    }
+
+    // chunk i+1 is launched before chunk i's control blocks are inspected
+    const long max_chunks = (long)o.max_iterations / (4 * passes) + 3;
+    long launched = 0;
+    bool finished = false;
+    auto all_done = [&](const Ctl *c) {
+        for (int i = 0; i < count; i++)
+            if (!c[i].done) return false;
+        return true;
+    };
+    while (!finished) {
+        if (launched >= max_chunks) {
+            set_error("batched tile solve: chunk budget exceeded without every grid done");
+            return PCD_TIMEOUT;
+        }
+        PCD_CUDA(cudaGraphLaunch(exec, s));
+        count_launches(passes + 2);
+        const int slot = (int)(launched & 1);
+        PCD_CUDA(cudaMemcpyAsync(ws.ctl_host + (size_t)slot * count, ws.ctl, sizeof(Ctl) * count,
+                                 cudaMemcpyDeviceToHost, s));
+        PCD_CUDA(cudaEventRecord(ws.ev[slot], s));
+        launched++;
+        if (launched >= 2) {
+            const int prev = (int)((launched - 2) & 1);
+            PCD_CUDA(cudaEventSynchronize(ws.ev[prev]));
+            if (all_done(ws.ctl_host + (size_t)prev * count)) finished = true;
+        }
+    }
+    PCD_CUDA(cudaEventRecord(ws.t1, s));
+    PCD_CUDA(cudaMemcpyAsync(ws.ctl_host, ws.ctl, sizeof(Ctl) * count, cudaMemcpyDeviceToHost, s));
+    PCD_CUDA(cudaStreamSynchronize(s));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, ws.t0, ws.t1);
+    int all = 1;
+    long long cell_sweeps = 0;
+    for (int i = 0; i < count; i++) {
+        const Ctl &c = ws.ctl_host[i];
+        if (stats) {
+            stats[i].sweeps = c.sweeps;
+            stats[i].converged = c.converged;
+            stats[i].rel_residual = c.rel;
+            stats[i].cycles = c.checks;
+        }
+        all &= c.converged;
+        cell_sweeps += (long long)inst[i].width * inst[i].height * c.sweeps;
+    }
+    if (bstats) {
+        bstats->device_ms = ms;
+        bstats->clusters = 0;
+        bstats->cluster_size = 0;
+        bstats->smem_bytes = (long long)smem;
+        bstats->cell_sweeps = cell_sweeps;
+        bstats->check_every = 4 * passes;
+        bstats->refine_drop = 0.0;
+        bstats->tuned = 0;
+    }
+    return all ? PCD_OK : PCD_NOT_CONVERGED;
+}
+
 }  // namespace pcd

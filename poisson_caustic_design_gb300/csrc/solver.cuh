@@ -107,6 +107,32 @@ struct SolverWorkspace {
     void release();
 };
 
+// Workspace of the batched tile solve (every grid of a batch in one tile
+// pass per launch); grows on demand.
+struct TileBatchWorkspace {
+    float *arena = nullptr;     // [all e][all e'][all r32], each grid H x ld
+    size_t arena_floats = 0;
+    Ctl *ctl = nullptr;         // one control block per grid
+    Ctl *ctl_host = nullptr;    // pinned, 2 slots of cap blocks
+    double *partials = nullptr; // residual partials per grid
+    void *jobs = nullptr;       // TileJob[cap] (device)
+    void *rjobs = nullptr;      // refine descriptors [cap] (device)
+    unsigned *counter = nullptr; // last-CTA counter of the batched pass
+    int cap = 0;
+    cudaEvent_t ev[2] = {nullptr, nullptr};
+    cudaEvent_t t0 = nullptr, t1 = nullptr;
+    std::map<std::vector<long long>, cudaGraphExec_t> graphs;
+    int reserve(size_t floats, int count);
+    void release();
+};
+
+// Mixed-precision batch solve (relative-residual stop) on batched tile
+// passes: every grid's width a multiple of 8 and ld of 4.  PCD_BAD_ARG
+// without device work when a grid does not qualify.
+int batch_tiles_solve(TileBatchWorkspace &ws, int dev, const pcd_instance *inst, int count, const pcd_solve_opts &o,
+                      pcd_instance_stats *stats, pcd_batch_stats *bstats, cudaStream_t s);
+bool batch_tiles_apply(const pcd_instance *inst, int count);
+
 // ||b - L phi|| / ||b|| (FP64) of a given phi
 int residual_rel(SolverWorkspace &ws, const double *b, const double *phi, int W, int H, int ld, cudaStream_t s,
                  double *rel);

@@ -219,6 +219,7 @@ int BatchWorkspace::reserve_inst(int count)
 
 void BatchWorkspace::release()
 {
+    tiles.release();
     for (auto &kv : graphs) cudaGraphExecDestroy(kv.second);
     graphs.clear();
     if (d_inst) cudaFree(d_inst);
@@ -261,6 +262,8 @@ int batch_solve_device(BatchWorkspace &ws, int dev, const pcd_instance *inst, in
             return PCD_BAD_ARG;
         }
     }
+    if (cluster == 0 && o.schedule != PCD_SCHED_CLUSTER && batch_tiles_apply(inst, count))
+        return batch_tiles_solve(ws.tiles, dev, inst, count, o, stats, bstats, s);
     PCD_TRY(ws.reserve_inst(count));
 
     // largest first (cost ~ cells x sweeps ~ W*H*max(W,H))

@@ -41,11 +41,14 @@ struct BatchWorkspace {
     unsigned *counter = nullptr;
     cudaEvent_t t0 = nullptr, t1 = nullptr;
     std::map<std::vector<long long>, cudaGraphExec_t> graphs;
+    TileBatchWorkspace tiles;   // the batched tile form
     int reserve_inst(int count);
     void release();
 };
 
-// cluster: CTAs per cluster (16 or 8; 0 = 16)
+// Grids whose widths are all multiples of 8 (ld of 4) run on batched tile
+// passes unless the schedule is PCD_SCHED_CLUSTER or a cluster size is given;
+// the others on clusters.  cluster: CTAs per cluster (16 or 8; 0 = 16)
 int batch_solve_device(BatchWorkspace &ws, int dev, const pcd_instance *inst, int count, const pcd_solve_opts &o,
                        pcd_instance_stats *stats, pcd_batch_stats *bstats, cudaStream_t s, int cluster = 0);
 

@@ -24,6 +24,7 @@
 // FP64 residual then decides convergence.
 #include <algorithm>
 #include <cooperative_groups.h>
+#include <string>
 
 #include "sor_cluster.cuh"
 #include "sor_planes.cuh"
@@ -655,6 +656,47 @@ int launch_tile(const TilePlan &p, const float *ein, float *eout, const float *r
     using Fn = void (*)(const float *, float *, const float *, Ctl *, SolveArgs, int, int, int, int);
     reinterpret_cast<Fn>(const_cast<void *>(fn))<<<p.grid, kRRThreads, p.smem, s>>>(ein, eout, r32, ctl, a, p.ncol,
                                                                                     p.nrow, nsw, out_idx);
+    return PCD_OK;
+}
+
+void tile_counts(int W, int H, int *ncol, int *nrow)
+{
+    constexpr int L = 4, NQ = 1, K = 4;
+    *ncol = ceil_div(W / 8, 32 * NQ - 2);
+    *nrow = ceil_div(H, kRRWarps * L - 4 * K);
+}
+
+int tile_batch_config(int dev, int njobs, size_t *smem, int *grid)
+{
+    if (njobs < 1 || njobs > kTileBatchJobsMax) {
+        set_error("batched tile pass: 1 to " + std::to_string(kTileBatchJobsMax) + " grids");
+        return PCD_BAD_ARG;
+    }
+    const void *fn = (const void *)k_sor_tile_batch<4, 4, 1>;
+    const size_t base = tile_floats(4, 1) * sizeof(float), per_job = sizeof(TileJob) + sizeof(int);
+    const size_t most = base + kTileBatchJobsMax * per_job, bytes = base + (size_t)njobs * per_job;
+    int sms = 0, bps = 0;
+    PCD_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    PCD_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)most));
+    PCD_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, fn, kRRThreads, bytes));
+    if (bps < 1) {
+        set_error("batched tile pass: the kernel does not fit on an SM");
+        return PCD_BAD_ARG;
+    }
+    *smem = bytes;
+    *grid = sms * bps;
+    return PCD_OK;
+}
+
+int launch_tile_batch(const TileJob *d_jobs, int njobs, int ntiles, int nsw, int par, int grid, size_t smem,
+                      unsigned *counter, cudaStream_t s)
+{
+    if (njobs < 1 || njobs > kTileBatchJobsMax || ntiles < 1 || nsw < 1 || nsw > 4) {
+        set_error("batched tile pass: bad arguments");
+        return PCD_BAD_ARG;
+    }
+    k_sor_tile_batch<4, 4, 1>
+        <<<std::min(grid, ntiles), kRRThreads, smem, s>>>(d_jobs, njobs, ntiles, nsw, par, counter);
     return PCD_OK;
 }
 

@@ -51,6 +51,33 @@ struct TilePlan {
     size_t smem = 0;
 };
 
+// One grid of a batched tile pass (the 64 x 256-cell tile form, 4 sweeps per
+// pass at most).
+struct TileJob {
+    float *ea, *eb;      // FP32 correction buffers (ping-pong)
+    const float *r32;    // FP32 right-hand side
+    Ctl *ctl;            // the grid's control block
+    int W, H, ld;        // W a multiple of 8, ld of 4
+    int ncol, nrow;      // tiles (tile_counts)
+    int tile0;           // first global tile index of the grid
+    int max_iter;
+    float w32[5];        // omega / cnt
+};
+static_assert(sizeof(TileJob) % 8 == 0, "job table copied to shared memory in words");
+
+// Tiles of a W x H grid in the batched form.
+void tile_counts(int W, int H, int *ncol, int *nrow);
+// Most grids in one batched pass (the job table sits in shared memory).
+constexpr int kTileBatchJobsMax = 1024;
+// Dynamic shared memory of the batched pass for njobs grids and its
+// persistent grid.
+int tile_batch_config(int dev, int njobs, size_t *smem, int *grid);
+// One batched pass of nsw <= 4 sweeps over ntiles tiles of njobs grids
+// (d_jobs on the device, tile0 ascending); parity par reads ea (0) or eb.
+// counter: a device word that is zero between passes.
+int launch_tile_batch(const TileJob *d_jobs, int njobs, int ntiles, int nsw, int par, int grid, size_t smem,
+                      unsigned *counter, cudaStream_t s);
+
 // The plan for a W x H grid with leading dimension ld (W a multiple of 8, ld
 // of 4); depth = sweeps per pass (2 or 4; 0: 4).  PCD_BAD_ARG when no form
 // applies.

@@ -81,7 +81,8 @@ def test_autotuned_batch(tctx):
     ps = [torch.zeros_like(b) for b in bs]
     o = pcd.SolveOptions(stop=pcd.STOP_REL_RESIDUAL, tol=1e-6, omega=-1.0, warm_start=0)
     per, bst = pcd.batch_solve(tctx, bs, ps, o)
-    assert bst["tuned"] == 1 and bst["cluster_size"] in (8, 16)
+    # 16- or 8-CTA clusters, or (cluster size 0) the batched tile passes
+    assert bst["tuned"] == 1 and bst["cluster_size"] in (0, 8, 16)
     assert all(x["converged"] and x["rel_residual"] <= 1e-6 for x in per)
     trials = tctx.autotune_info()["trials"]
     assert trials >= 2

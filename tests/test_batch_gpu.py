@@ -96,3 +96,73 @@ def test_batch_rejects_bad_instances(ctx):
     b = torch.zeros((16, 16), dtype=torch.float64, device="cuda")
     with pytest.raises(pcd.PCDError):
         pcd.batch_solve(ctx, [b], [torch.zeros_like(b)])      # height < 32
+
+
+TILE_SIZES = [(64, 64), (96, 64), (128, 128), (256, 200), (512, 512), (1024, 1024), (504, 33), (1024, 300)]
+
+
+def test_batch_tile_form_matches_cluster_form(ctx):
+    """Grids whose widths are multiples of 8 run on batched tile passes (every
+    grid's tiles in one launch per pass, FP64 refreshes batched per chunk):
+    each converges to the tolerance against the exact solve, as on the
+    cluster form (schedule CLUSTER), with a similar sweep count."""
+    import torch
+
+    import oracle
+    import poisson_caustic_design_gb300 as pcd
+
+    rhs = [pcd.inputs.poisson_rhs(w, 80 + i, "binary" if i % 2 else "gaussian", m=h)
+           for i, (w, h) in enumerate(TILE_SIZES)]
+    bs = [torch.from_numpy(b).cuda() for b in rhs]
+    res = {}
+    for sched in (0, 3):
+        phis = [torch.full_like(b, 3.0) for b in bs]
+        opts = pcd.SolveOptions(stop=pcd.STOP_REL_RESIDUAL, tol=1e-8, max_iterations=200000, omega=-1.0,
+                                warm_start=False, schedule=sched)
+        per, bst = pcd.batch_solve(ctx, bs, phis, opts)
+        torch.cuda.synchronize()
+        assert bst["status"] == 0
+        assert (bst["clusters"] == 0) if sched == 0 else (bst["clusters"] >= 1)
+        port = oracle.Port()
+        for i, (b, p) in enumerate(zip(rhs, phis)):
+            assert per[i]["converged"] == 1, (TILE_SIZES[i], per[i])
+            phi = p.cpu().numpy()
+            _, rn, bn, _ = port.residual(b, phi)
+            assert rn / bn <= 1.05e-8, (TILE_SIZES[i], rn / bn, per[i])
+            assert abs(rn / bn - per[i]["rel_residual"]) <= 1e-3 * per[i]["rel_residual"] + 1e-15
+            assert oracle.rel_err_mod_const(phi, oracle.dct_solve(b))[0] < 1e-6, TILE_SIZES[i]
+        res[sched] = [x["sweeps"] for x in per]
+    for (w, h), st, sc in zip(TILE_SIZES, res[0], res[3]):
+        assert st <= 1.3 * sc + 64, ((w, h), st, sc)
+
+
+def test_batch_tile_form_padded_rows_and_sweep_cap(ctx):
+    """Batched tile passes on padded rows (ld a multiple of 4 above the width)
+    stop every grid at max_iterations exactly, with the iterate of the
+    single-grid tile schedule (the same FP64 refreshes every 64 sweeps)."""
+    import torch
+
+    import poisson_caustic_design_gb300 as pcd
+
+    shapes = [(256, 100, 260), (128, 70, 132), (512, 40, 520)]
+    bs, phis = [], []
+    for i, (w, h, ld) in enumerate(shapes):
+        full = torch.zeros((h, ld), dtype=torch.float64, device="cuda")
+        full[:, :w] = torch.from_numpy(pcd.inputs.poisson_rhs(w, 90 + i, "gaussian", m=h)).cuda()
+        bs.append(full[:, :w])
+        phis.append(torch.zeros((h, ld), dtype=torch.float64, device="cuda")[:, :w])
+    opts = pcd.SolveOptions(stop=pcd.STOP_REL_RESIDUAL, tol=1e-14, max_iterations=101, omega=-1.0,
+                            warm_start=False, refine_every=64)
+    per, bst = pcd.batch_solve(ctx, bs, phis, opts)
+    torch.cuda.synchronize()
+    assert bst["clusters"] == 0 and bst["status"] == 1
+    for (w, h, ld), b, p, x in zip(shapes, bs, phis, per):
+        assert x["sweeps"] == 101 and x["converged"] == 0, x
+        single = torch.zeros((h, ld), dtype=torch.float64, device="cuda")[:, :w]
+        st = ctx.solve_device(b, single, pcd.SolveOptions(stop=pcd.STOP_REL_RESIDUAL, tol=1e-14, max_iterations=101,
+                                                          omega=-1.0, precision=pcd.PREC_MIXED, schedule=6,
+                                                          refine_every=64, warm_start=0))
+        assert st["sweeps"] == 101 and st["schedule_used"] == 6
+        ref = single.cpu().numpy()
+        err = np.abs(p.cpu().numpy() - ref).max() / np.abs(ref).max()
+        assert err < 1e-6, ((w, h), err)
