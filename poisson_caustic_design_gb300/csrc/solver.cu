@@ -23,6 +23,7 @@
 // Sweeps are issued as CUDA-graph chunks; the stop flags live in device memory
 // and make the remaining kernels of a chunk return at once, so the host reads
 // the control block once per chunk and launches the next chunk speculatively.
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 
@@ -1210,8 +1211,10 @@ struct RefineJob {
     int blk0, nblk;
 };
 
-constexpr int kBatchRefineBlocks = 64;  // per grid at most
-constexpr int kBatchChunkPasses = 16;   // tile passes (of 4 sweeps) between FP64 refreshes
+// Blocks per grid of the batched FP64 refresh: about 4 cells per thread, so
+// that the large grids' FP64 work spreads over every SM.
+constexpr int kBatchRefineBlocks = 1024;
+constexpr int kBatchRefineCellsPerBlock = 4 * kThreads;
 
 __device__ __forceinline__ int refine_job(const RefineJob *jobs, int njobs, int blk)
 {
@@ -1254,13 +1257,15 @@ __global__ void __launch_bounds__(kThreads)
         const int y = (int)(t / W), x = (int)(t - (long)y * W);
         const long i = (long)y * ld + x;
         const double bi = J.b[i];
-        double sum = 0.0, cnt = 0.0;
-        if (x > 0) { cnt += 1.0; sum += J.phi[i - 1] + (double)e[i - 1]; }
-        if (y > 0) { cnt += 1.0; sum += J.phi[i - ld] + (double)e[i - ld]; }
-        if (x < W - 1) { cnt += 1.0; sum += J.phi[i + 1] + (double)e[i + 1]; }
-        if (y < H - 1) { cnt += 1.0; sum += J.phi[i + ld] + (double)e[i + ld]; }
+        // the neighbour sum in k_refine_residual's order; the count as an integer
+        double sum = 0.0;
+        int cnt = 0;
+        if (x > 0) { cnt++; sum += J.phi[i - 1] + (double)e[i - 1]; }
+        if (y > 0) { cnt++; sum += J.phi[i - ld] + (double)e[i - ld]; }
+        if (x < W - 1) { cnt++; sum += J.phi[i + 1] + (double)e[i + 1]; }
+        if (y < H - 1) { cnt++; sum += J.phi[i + ld] + (double)e[i + ld]; }
         const double xi = J.phi[i] + (double)e[i];
-        const double r = bi - (sum - cnt * xi);
+        const double r = bi - (sum - (double)cnt * xi);
         J.r32[i] = (float)r;
         if (isnan(bi)) continue;
         v[0] += r * r;
@@ -1393,18 +1398,26 @@ int batch_tiles_solve(TileBatchWorkspace &ws, int dev, const pcd_instance *inst,
     for (int i = 0; i < count; i++) per += (size_t)inst[i].height * inst[i].ld;
     PCD_TRY(ws.reserve(3 * per, count));
 
+    // largest grids first: their refresh blocks are dispatched first
+    std::vector<int> order(count);
+    for (int i = 0; i < count; i++) order[i] = i;
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
+        return (long)inst[x].width * inst[x].height > (long)inst[y].width * inst[y].height;
+    });
     std::vector<TileJob> tj((size_t)count);
     std::vector<RefineJob> rj((size_t)count);
     size_t off = 0;
-    int tiles = 0, blocks = 0;
-    for (int i = 0; i < count; i++) {
+    int tiles = 0, blocks = 0, maxdim = 0;
+    for (int k = 0; k < count; k++) {
+        const int i = order[k];
         const pcd_instance &q = inst[i];
-        TileJob &t = tj[i];
-        RefineJob &r = rj[i];
+        maxdim = std::max(maxdim, std::max(q.width, q.height));
+        TileJob &t = tj[k];
+        RefineJob &r = rj[k];
         t.ea = ws.arena + off;
         t.eb = ws.arena + per + off;
         t.r32 = ws.arena + 2 * per + off;
-        t.ctl = ws.ctl + i;
+        t.ctl = ws.ctl + k;
         t.W = q.width;
         t.H = q.height;
         t.ld = q.ld;
@@ -1420,18 +1433,23 @@ int batch_tiles_solve(TileBatchWorkspace &ws, int dev, const pcd_instance *inst,
         r.eb = t.eb;
         r.r32 = ws.arena + 2 * per + off;
         r.ctl = t.ctl;
-        r.partials = ws.partials + (size_t)3 * kBatchRefineBlocks * i;
+        r.partials = ws.partials + (size_t)3 * kBatchRefineBlocks * k;
         r.W = q.width;
         r.H = q.height;
         r.ld = q.ld;
         r.blk0 = blocks;
-        r.nblk = (int)std::min<long>(kBatchRefineBlocks, ((long)q.width * q.height + kThreads - 1) / kThreads);
+        r.nblk = (int)std::min<long>(kBatchRefineBlocks,
+                                     ((long)q.width * q.height + kBatchRefineCellsPerBlock - 1) /
+                                         kBatchRefineCellsPerBlock);
         blocks += r.nblk;
         off += (size_t)q.height * q.ld;
     }
     const TileJob *d_jobs = static_cast<const TileJob *>(ws.jobs);
     const RefineJob *d_rjobs = static_cast<const RefineJob *>(ws.rjobs);
-    const int passes = o.refine_every > 0 ? std::max(1, (o.refine_every + 3) / 4) : kBatchChunkPasses;
+    // tile passes (of 4 sweeps) between FP64 refreshes: 128 sweeps for the
+    // largest grids of 1024 cells or more, 32 for grids of 256 or less
+    const int passes =
+        o.refine_every > 0 ? std::max(1, (o.refine_every + 3) / 4) : std::max(8, std::min(32, maxdim / 32));
 
     PCD_CUDA(cudaEventRecord(ws.t0, s));
     PCD_CUDA(cudaMemcpyAsync(ws.jobs, tj.data(), sizeof(TileJob) * count, cudaMemcpyHostToDevice, s));
@@ -1521,8 +1539,9 @@ int batch_tiles_solve(TileBatchWorkspace &ws, int dev, const pcd_instance *inst,
     cudaEventElapsedTime(&ms, ws.t0, ws.t1);
     int all = 1;
     long long cell_sweeps = 0;
-    for (int i = 0; i < count; i++) {
-        const Ctl &c = ws.ctl_host[i];
+    for (int k = 0; k < count; k++) {
+        const int i = order[k];
+        const Ctl &c = ws.ctl_host[k];
         if (stats) {
             stats[i].sweeps = c.sweeps;
             stats[i].converged = c.converged;
