@@ -209,9 +209,14 @@ typedef struct {
 } pcd_batch_stats;
 
 /* Mixed precision (FP32 sweeps, FP64 defect correction) with the relative-
- * residual stop; opts->omega as in pcd_solve_opts, per instance.  Each 16-CTA
- * cluster takes instances from a work queue (largest first) and solves them
- * whole.  stats has `count` entries in the caller's order. */
+ * residual stop; opts->omega as in pcd_solve_opts, per instance.  When every
+ * width is a multiple of 8 and every ld of 4 (and at most 1024 instances),
+ * each launch runs up to 4 sweeps over the tiles of every instance that has
+ * not converged, with a batched FP64 refresh every refine_every sweeps (0:
+ * 32 to 128 by the largest side; batch_stats->check_every reports it,
+ * clusters = 0); otherwise, or with opts->schedule = PCD_SCHED_CLUSTER, each
+ * 16-CTA cluster takes instances from a work queue (largest first) and solves
+ * them whole.  stats has `count` entries in the caller's order. */
 int pcd_batch_solve_device(pcd_ctx *ctx, const pcd_instance *inst, int count, const pcd_solve_opts *opts,
                            pcd_instance_stats *stats, pcd_batch_stats *batch_stats, void *stream);
 
