@@ -58,6 +58,8 @@ def parse():
     ap.add_argument("--no-autotune", action="store_true", help="solve with the schedules' default settings")
     ap.add_argument("--stream-only", action="store_true",
                     help="only the 4096^2 sweep-roofline section (for profiling the stream kernel)")
+    ap.add_argument("--batch-only", action="store_true",
+                    help="one solve of the 64-grid batch and nothing else (for profiling the batched kernels)")
     ap.add_argument("--config4", action="store_true",
                     help="instead of the headline: the full caustic pipeline at a 1024^2 mesh on 4096^2 grids "
                          "(transport and height iterations, plain FP64 and mixed), one JSON line")
@@ -219,6 +221,14 @@ def run_reference(args, rank, world, pg):
     print(json.dumps(line), flush=True)
 
 
+def batch_instances(pcd):
+    """The 64-grid batch: sides drawn from {64, 96, 128, 256, 512, 1024}
+    (seed 2024), seeded Gaussian densities, on the current CUDA device."""
+    rs = np.random.default_rng(2024)
+    sizes = [int(rs.choice([64, 96, 128, 256, 512, 1024])) for _ in range(64)]
+    return sizes, [pcd.inputs.poisson_rhs_torch(n_, [5000 + i])[0].contiguous() for i, n_ in enumerate(sizes)]
+
+
 def stream_section(ctx, stream, peak):
     """Sweep rates on 4096^2, 256 sweeps per solve: FP32 stream passes and
     FP32 register-resident tile passes (12 B algorithmic per cell-sweep; the
@@ -268,6 +278,19 @@ def run_ours(args, rank, world, local, pg):
     # (trial solves on the first call of a shape, outside the timed region)
     ctx.set_autotune(not args.no_autotune)
     L = _lib.load()
+    if args.batch_only:
+        import torch
+
+        sizes, bb = batch_instances(pcd)
+        pp = [torch.zeros_like(x) for x in bb]
+        bopts = pcd.SolveOptions(stop=pcd.STOP_REL_RESIDUAL, tol=TOL, max_iterations=200000, omega=-1.0,
+                                 warm_start=0)
+        per, bst = pcd.batch_solve(ctx, bb, pp, bopts)
+        torch.cuda.synchronize(dev)
+        print(json.dumps({"batch_only": {"device_ms": bst["device_ms"], "clusters": bst["clusters"],
+                                         "all_converged": bool(all(x["converged"] for x in per))}}), flush=True)
+        ctx.close()
+        return
     if args.stream_only:
         peak, src = measured_hbm_peak()
         print(json.dumps({"roofline_stream_4096": stream_section(ctx, torch.cuda.current_stream(dev), peak),
@@ -398,13 +421,12 @@ def run_ours(args, rank, world, local, pg):
                     "r32 in shared memory): the kernel is bound by FP32 issue, block and cluster barriers, not "
                     "HBM; DRAM traffic per launch is the band load and store (ncu summary under profiles/)"}
 
-    # batched configuration: 64 instances, sizes uniform in {64..1024}^2, one
-    # persistent cluster launch (CUDA graph); FP32 sweeps, FP64 residuals
+    # batched configuration: 64 instances, sizes uniform in {64..1024}^2,
+    # batched tile passes or the cluster form (CUDA graphs, the autotuner
+    # picks); FP32 sweeps, FP64 residuals
     batched = None
     if not args.no_batch and not args.headline_only:
-        rs = np.random.default_rng(2024)
-        sizes = [int(rs.choice([64, 96, 128, 256, 512, 1024])) for _ in range(64)]
-        bb = [pcd.inputs.poisson_rhs_torch(n_, [5000 + i])[0].contiguous() for i, n_ in enumerate(sizes)]
+        sizes, bb = batch_instances(pcd)
         pp = [torch.zeros_like(x) for x in bb]
         bopts = pcd.SolveOptions(stop=pcd.STOP_REL_RESIDUAL, tol=TOL, max_iterations=200000, omega=-1.0, warm_start=0)
         for w in range(max(1, args.warmup // 2)):
@@ -424,6 +446,7 @@ def run_ours(args, rank, world, local, pg):
                    "alg_gbs": 12.0 * bst["cell_sweeps"] / (bms * 1e-3) / 1e9,
                    "all_converged": bool(all(x["converged"] for x in per)),
                    "max_rel_residual": float(max(x["rel_residual"] for x in per)),
+                   "form": "tiles" if bst["clusters"] == 0 else "clusters",
                    "clusters": bst["clusters"], "cluster_size": bst["cluster_size"],
                    "check_every": bst["check_every"], "refine_drop": bst["refine_drop"], "autotuned": bool(bst["tuned"])}
         del bb, pp
