@@ -26,6 +26,10 @@
 // the rows of its next tile (bulk prefetches), so that tile's loads hit L2.
 // The CTA that finishes last closes the pass (end_of_sweep with kr sweeps);
 // with TRACK the pass reports the largest |update| of its last sweep.
+//
+// k_sor_tile_batch runs the same tiles for many grids at once: the grids'
+// tiles are numbered one after the other (TileJob::tile0) and the persistent
+// CTAs stride over all of them, skipping the grids whose solves have halted.
 
 // Shared floats of one tile: edge rows [2 colours][16 warps][2 sides] and the
 // -r32 planes [2 colours][R rows], each row KS = 128 NQ slots.
