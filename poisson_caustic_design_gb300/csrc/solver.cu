@@ -1446,10 +1446,11 @@ int batch_tiles_solve(TileBatchWorkspace &ws, int dev, const pcd_instance *inst,
     }
     const TileJob *d_jobs = static_cast<const TileJob *>(ws.jobs);
     const RefineJob *d_rjobs = static_cast<const RefineJob *>(ws.rjobs);
-    // tile passes (of 4 sweeps) between FP64 refreshes: 128 sweeps for the
-    // largest grids of 1024 cells or more, 32 for grids of 256 or less
-    const int passes =
-        o.refine_every > 0 ? std::max(1, (o.refine_every + 3) / 4) : std::max(8, std::min(32, maxdim / 32));
+    // sweeps between FP64 refreshes (passes of 4, the last one shorter):
+    // refine_every, else 128 when the largest side is 1024 or more, down to
+    // 32 when it is 256 or less
+    const int chunk = o.refine_every > 0 ? o.refine_every : 4 * std::max(8, std::min(32, maxdim / 32));
+    const int passes = (chunk + 3) / 4;
 
     PCD_CUDA(cudaEventRecord(ws.t0, s));
     PCD_CUDA(cudaMemcpyAsync(ws.jobs, tj.data(), sizeof(TileJob) * count, cudaMemcpyHostToDevice, s));
@@ -1467,7 +1468,7 @@ int batch_tiles_solve(TileBatchWorkspace &ws, int dev, const pcd_instance *inst,
     PCD_LAUNCHED(2);
 
     // one CUDA graph per batch signature: the chunk's passes and the refresh
-    std::vector<long long> key = {count, tiles, blocks, passes, grid, (long long)smem,
+    std::vector<long long> key = {count, tiles, blocks, chunk, grid, (long long)smem,
                                   (long long)(uintptr_t)ws.jobs, (long long)(uintptr_t)ws.rjobs};
     {
         long long tb;
@@ -1483,7 +1484,8 @@ int batch_tiles_solve(TileBatchWorkspace &ws, int dev, const pcd_instance *inst,
         PCD_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
         int st = PCD_OK;
         for (int k = 0; k < passes && st == PCD_OK; k++)
-            st = launch_tile_batch(d_jobs, count, tiles, 4, k & 1, grid, smem, ws.counter, s);
+            st = launch_tile_batch(d_jobs, count, tiles, std::min(4, chunk - 4 * k), k & 1, grid, smem, ws.counter,
+                                   s);
         k_batch_refine_residual<<<blocks, kThreads, 0, s>>>(d_rjobs, count, o.tol, 0);
         k_batch_refine_update<<<blocks, kThreads, 0, s>>>(d_rjobs, count);
         cudaError_t ce = cudaStreamEndCapture(s, &g);
@@ -1506,7 +1508,7 @@ int batch_tiles_solve(TileBatchWorkspace &ws, int dev, const pcd_instance *inst,
     }
 
     // chunk i+1 is launched before chunk i's control blocks are inspected
-    const long max_chunks = (long)o.max_iterations / (4 * passes) + 3;
+    const long max_chunks = (long)o.max_iterations / chunk + 3;
     long launched = 0;
     bool finished = false;
     auto all_done = [&](const Ctl *c) {
@@ -1557,7 +1559,7 @@ int batch_tiles_solve(TileBatchWorkspace &ws, int dev, const pcd_instance *inst,
         bstats->cluster_size = 0;
         bstats->smem_bytes = (long long)smem;
         bstats->cell_sweeps = cell_sweeps;
-        bstats->check_every = 4 * passes;
+        bstats->check_every = chunk;
         bstats->refine_drop = 0.0;
         bstats->tuned = 0;
     }
