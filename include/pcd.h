@@ -155,6 +155,16 @@ const char *pcd_status_string(int status);
 int pcd_solve_opts_default(pcd_solve_opts *opts);
 /* Number of kernels this library launched in this process (monotonic). */
 unsigned long long pcd_kernel_launches(void);
+/* Bounded device waits (no counterpart in the reference, whose solver has no
+ * device waits).  The persistent schedule's CTAs wait for their neighbours'
+ * epoch flags and for a grid barrier; each wait gives up after `polls` polls
+ * (0 = the default 2^24, about half a second), records PCD_TIMEOUT and every
+ * CTA returns, leaving the context usable; the solve returns PCD_TIMEOUT.
+ * withhold_first_flag = 1 is the failure test's switch: the first CTA never
+ * raises its epoch flag, a flag that nothing else sets, so a neighbour's wait
+ * runs out on purpose.  Both stay in force for later solves on the context
+ * until changed. */
+int pcd_ctx_set_wait_limit(pcd_ctx *ctx, long long polls, int withhold_first_flag);
 
 /* ---- Poisson solve ------------------------------------------------------ */
 /* Drop-in for poisson_solver(D, phi, width, height, max_iterations,
@@ -185,7 +195,9 @@ int pcd_poisson_solve_device(pcd_ctx *ctx, const double *b, double *phi, int wid
  * call; this runs many independent grids of uneven sizes in one persistent
  * launch, captured in a CUDA graph) ------------------------------------- */
 typedef struct {
-    int width, height, ld;   /* ld >= width; 32 <= height, width <= 4096 */
+    int width, height, ld;   /* ld >= width.  Batched tile form: width a multiple of 8, ld of 4,
+                                any height.  Cluster form: width <= 4096, height >= 2 x the
+                                cluster size (32 with 16-CTA clusters) */
     const double *b;         /* device, right-hand side */
     double *phi;             /* device, solution (warm start when opts->warm_start) */
 } pcd_instance;
@@ -319,9 +331,12 @@ int pcd_divergence_device(pcd_ctx *ctx, const double *nx, const double *ny, doub
  * CURRENT device, enqueued on `stream` (NULL = legacy default stream).  Its
  * scratch is a static device array of 2*16384+2 doubles held by every GPU
  * that loads the library until exit, so height must be <= 16384 (else
- * PCD_BAD_ARG).  The first call on a device looks up that array's device
- * address (make it before any stream capture).  All calls share the array:
- * calls that overlap on the GPU race and must be serialised by the caller. */
+ * PCD_BAD_ARG).  A call on a stream that is not capturing looks that array's
+ * device address up afresh; a call on a capturing stream reuses the address
+ * of the last such lookup on the device, so make one call on each device
+ * before any stream capture, and again after a cudaDeviceReset.  All calls
+ * share the array: calls that overlap on the GPU race and must be serialised
+ * by the caller. */
 int pcd_subtract_average_noalloc(double *g, int width, int height, void *stream);
 
 /* ---- Caustic_design ----------------------------------------------------- */

@@ -29,7 +29,8 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 PORT_SO = os.path.join(HERE, "_build", "libpcd_oracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libpcd_ref.so")
-REF_TREE = "/root/reference"
+# the reference tree: $PCD_REFERENCE when set, else where this container mounts it
+REF_TREE = os.environ.get("PCD_REFERENCE", "/root/reference")
 
 _dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
 
@@ -40,7 +41,7 @@ def build(ref: bool | None = None) -> None:
     if ref is None:
         ref = os.path.isdir(os.path.join(REF_TREE, "src"))
     if ref:
-        subprocess.run(["make", "-s", "-C", HERE, "ref"], check=True)
+        subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={REF_TREE}"], check=True)
 
 
 def _f64(a):

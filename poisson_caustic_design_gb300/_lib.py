@@ -136,6 +136,7 @@ SIGNATURES = {
     "pcd_batch_solve_device": (C.c_int, [_vp, C.POINTER(Instance), C.c_int, C.POINTER(SolveOpts),
                                          C.POINTER(InstanceStats), C.POINTER(BatchStats), _vp]),
     "pcd_ctx_set_autotune": (C.c_int, [_vp, C.c_int]),
+    "pcd_ctx_set_wait_limit": (C.c_int, [_vp, C.c_longlong, C.c_int]),
     "pcd_write_solid_obj": (C.c_int, [_dp, _dp, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, C.c_char_p]),
     "pcd_write_grid_svg": (C.c_int, [_dp, C.c_int, C.c_int, C.c_double, C.c_double, C.c_char_p, C.c_double]),
     "pcd_write_heightmap_json": (C.c_int, [_dp, C.c_int, C.c_int, C.c_char_p]),

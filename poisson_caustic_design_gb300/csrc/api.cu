@@ -111,7 +111,10 @@ int judge_prepare(pcd_ctx *ctx, int W, int H, int ld, cudaStream_t s)
     // nothing ran during the capture: count the kernels at each replay instead
     J.launches = g_launches.load() - n0;
     g_launches.fetch_sub(J.launches, std::memory_order_relaxed);
-    if (st != PCD_OK) return st;
+    if (st != PCD_OK) {
+        if (ce == cudaSuccess) cudaGraphDestroy(g);
+        return st;
+    }
     if (ce != cudaSuccess) {
         set_error(std::string("judge graph capture: ") + cudaGetErrorString(ce));
         return PCD_DEVICE_ERROR;
@@ -342,6 +345,18 @@ int pcd_ctx_destroy(pcd_ctx *ctx)
 }
 
 void *pcd_ctx_stream(pcd_ctx *ctx) { return ctx ? (void *)ctx->stream : nullptr; }
+
+int pcd_ctx_set_wait_limit(pcd_ctx *ctx, long long polls, int withhold_first_flag)
+{
+    if (!ctx || polls < 0) {
+        set_error("pcd_ctx_set_wait_limit: null context or negative poll count");
+        return PCD_BAD_ARG;
+    }
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    ctx->solver.wait_limit = polls;
+    ctx->solver.withhold_flag = withhold_first_flag ? 1 : 0;
+    return PCD_OK;
+}
 
 int pcd_poisson_solve_device(pcd_ctx *ctx, const double *b, double *phi, int width, int height, int ld,
                              const pcd_solve_opts *opts, pcd_solve_stats *stats, void *stream)

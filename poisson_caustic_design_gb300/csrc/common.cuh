@@ -86,7 +86,9 @@ __device__ __forceinline__ void block_reduce(double (&v)[N])
     if (wid == 0) {
 #pragma unroll
         for (int k = 0; k < N; k++) {
-            double x = lane < nw ? sm[lane][k] : (((OPS >> k) & 1u) ? 0.0 : 0.0);
+            // lanes past the last warp hold each slot's identity: 0 for a sum,
+            // -inf for a max (so signed maxima come out right as well)
+            double x = lane < nw ? sm[lane][k] : (((OPS >> k) & 1u) ? -__longlong_as_double(0x7ff0000000000000ll) : 0.0);
             v[k] = ((OPS >> k) & 1u) ? warp_max(x) : warp_sum(x);
         }
     }

@@ -23,10 +23,15 @@
 // serialised by the caller.
 //
 // The host side never dereferences the array's name: in host code that name
-// is only a stand-in for the device variable.  The device address is looked
-// up once per device with cudaGetSymbolAddress, with that device current, by
-// the first call made on the device; make that first call before any stream
-// capture.
+// is only a stand-in for the device variable.  Its device address comes from
+// cudaGetSymbolAddress with the device current.  A call on a stream that is
+// not capturing looks it up again every time (a host lookup, no device work),
+// so a cudaDeviceReset or a released primary context, after which the module
+// is loaded again and the array may sit elsewhere, leaves no stale address
+// behind.  A call made while its stream is capturing reuses the address that
+// the last non-capturing call on that device found (looking a symbol up can
+// load the module, which a capture does not allow): make one call on the
+// device before any stream capture, and again after a device reset.
 #include <mutex>
 
 #include "common.cuh"
@@ -82,8 +87,9 @@ __global__ void __launch_bounds__(kNoallocThreads) k_subtract(double *__restrict
     }
 }
 
-// Device address of g_noalloc_scratch on the current device, looked up once.
-int scratch_address(double **out)
+// Device address of g_noalloc_scratch on the current device: looked up again
+// unless `s` is capturing, then the address of the last lookup on the device.
+int scratch_address(cudaStream_t s, double **out)
 {
     int dev = 0;
     PCD_CUDA(cudaGetDevice(&dev));
@@ -91,11 +97,16 @@ int scratch_address(double **out)
         set_error("pcd_subtract_average_noalloc: device index out of range");
         return PCD_BAD_ARG;
     }
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    PCD_CUDA(cudaStreamIsCapturing(s, &cs));
     std::lock_guard<std::mutex> lk(g_setup_mu);
-    if (!g_scratch_addr[dev]) {
+    if (cs == cudaStreamCaptureStatusNone) {
         void *p = nullptr;
         PCD_CUDA(cudaGetSymbolAddress(&p, g_noalloc_scratch));
         g_scratch_addr[dev] = static_cast<double *>(p);
+    } else if (!g_scratch_addr[dev]) {
+        set_error("pcd_subtract_average_noalloc: the first call on a device must come before any stream capture");
+        return PCD_BAD_ARG;
     }
     *out = g_scratch_addr[dev];
     return PCD_OK;
@@ -119,8 +130,8 @@ extern "C" int pcd_subtract_average_noalloc(double *g, int width, int height, vo
         return PCD_BAD_ARG;
     }
     double *scratch = nullptr;
-    PCD_TRY(scratch_address(&scratch));
     cudaStream_t s = (cudaStream_t)stream;
+    PCD_TRY(scratch_address(s, &scratch));
     const long n = (long)width * height;
     k_row_sums<<<height, kNoallocThreads, 0, s>>>(g, width, scratch);
     PCD_LAUNCHED(1);

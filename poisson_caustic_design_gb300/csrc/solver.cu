@@ -760,7 +760,10 @@ int get_chunk_graph(SolverWorkspace &ws, const double *b, double *phi, const Sol
     int st = masked ? enqueue_chunk<true>(ws, b, phi, a, precision, sweeps, s, &nodes, PCD_SCHED_LAUNCHES, sp)
                     : enqueue_chunk<false>(ws, b, phi, a, precision, sweeps, s, &nodes, sched, sp);
     cudaError_t ce = cudaStreamEndCapture(s, &g);
-    if (st != PCD_OK) return st;
+    if (st != PCD_OK) {
+        if (ce == cudaSuccess) cudaGraphDestroy(g);
+        return st;
+    }
     if (ce != cudaSuccess) {
         set_error(std::string("cudaStreamEndCapture: ") + cudaGetErrorString(ce));
         return PCD_DEVICE_ERROR;
@@ -823,7 +826,8 @@ int solve_persistent(SolverWorkspace &ws, const double *b, double *phi, const So
     else pa.check_every = 32;
     if (mixed && o.refine_every > 0 && o.refine_every < pa.check_every) pa.check_every = o.refine_every;
     for (int c = 0; c < 5; c++) { pa.w64[c] = a.w64[c]; pa.w32[c] = a.w32[c]; }
-    pa.spin_limit = 1ll << 24;
+    pa.spin_limit = ws.wait_limit > 0 ? ws.wait_limit : 1ll << 24;
+    pa.withhold = ws.withhold_flag;
     PCD_CUDA(cudaEventRecord(ws.k0, s));
     PCD_TRY(launch_persist(pa, mixed, smem, s));
     PCD_CUDA(cudaEventRecord(ws.k1, s));
@@ -1489,7 +1493,10 @@ int batch_tiles_solve(TileBatchWorkspace &ws, int dev, const pcd_instance *inst,
         k_batch_refine_residual<<<blocks, kThreads, 0, s>>>(d_rjobs, count, o.tol, 0);
         k_batch_refine_update<<<blocks, kThreads, 0, s>>>(d_rjobs, count);
         cudaError_t ce = cudaStreamEndCapture(s, &g);
-        if (st != PCD_OK) return st;
+        if (st != PCD_OK) {
+            if (ce == cudaSuccess) cudaGraphDestroy(g);
+            return st;
+        }
         if (ce != cudaSuccess) {
             set_error(std::string("batched tile graph capture: ") + cudaGetErrorString(ce));
             return PCD_DEVICE_ERROR;

@@ -96,6 +96,10 @@ struct SolverWorkspace {
     int max_ctas = 0;
     int stripe_resident = 0;    // resident stripe blocks (SMs x blocks per SM)
     double *part = nullptr;     // check partials
+    // bounded waits of the persistent schedule: polls before a flag wait gives
+    // up (0: 2^24), and the failure test's withheld flag (pcd_ctx_set_wait_limit)
+    long long wait_limit = 0;
+    int withhold_flag = 0;
 
     struct GraphEntry {
         cudaGraphExec_t exec;

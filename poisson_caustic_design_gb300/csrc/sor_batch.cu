@@ -252,18 +252,21 @@ int batch_solve_device(BatchWorkspace &ws, int dev, const pcd_instance *inst, in
         set_error("pcd_batch_solve_device: cluster size must be 8 or 16");
         return PCD_BAD_ARG;
     }
+    // the batched tile passes take any height and width (widths multiples of
+    // 8); the cluster form's limits below apply only to batches it solves
+    if (cluster == 0 && o.schedule != PCD_SCHED_CLUSTER && batch_tiles_apply(inst, count))
+        return batch_tiles_solve(ws.tiles, dev, inst, count, o, stats, bstats, s);
     const int C = cluster ? cluster : 16;
     for (int i = 0; i < count; i++) {
         const pcd_instance &q = inst[i];
         if (!q.b || !q.phi || q.width < 2 || q.height < 2 * C || q.ld < q.width ||
             plane_stride(q.width) / 2 > kBatchThreads) {
             set_error("pcd_batch_solve_device: instance " + std::to_string(i) +
-                      " needs 2 <= width <= 4096, height >= 2 x cluster size, ld >= width and device arrays");
+                      " needs 2 <= width <= 4096, height >= 2 x cluster size, ld >= width and device arrays "
+                      "(the cluster form; the tile form takes widths that are multiples of 8 and ld of 4)");
             return PCD_BAD_ARG;
         }
     }
-    if (cluster == 0 && o.schedule != PCD_SCHED_CLUSTER && batch_tiles_apply(inst, count))
-        return batch_tiles_solve(ws.tiles, dev, inst, count, o, stats, bstats, s);
     PCD_TRY(ws.reserve_inst(count));
 
     // largest first (cost ~ cells x sweeps ~ W*H*max(W,H))
@@ -376,6 +379,7 @@ int batch_solve_device(BatchWorkspace &ws, int dev, const pcd_instance *inst, in
         cudaMemcpyAsync(ws.h_inst, ws.d_inst, sizeof(BatchInst) * count, cudaMemcpyDeviceToHost, s);
         cudaError_t ce = cudaStreamEndCapture(s, &gph);
         if (le != cudaSuccess || ce != cudaSuccess) {
+            if (ce == cudaSuccess) cudaGraphDestroy(gph);
             set_error(std::string("batch graph capture: ") + cudaGetErrorString(le != cudaSuccess ? le : ce));
             return PCD_DEVICE_ERROR;
         }

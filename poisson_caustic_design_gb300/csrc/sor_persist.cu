@@ -103,7 +103,7 @@ __device__ void publish(const PersistArgs &a, const T *s, int n, int slot, unsig
         dst1[c] = s[(size_t)n * a.W + c];
     }
     __syncthreads();
-    if (threadIdx.x == 0) {
+    if (threadIdx.x == 0 && !(a.withhold && blockIdx.x == 0)) {
         __threadfence();
         st_release(&a.flags[blockIdx.x], ep);
     }

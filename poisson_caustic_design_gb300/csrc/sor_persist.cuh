@@ -22,6 +22,8 @@ struct PersistArgs {
     double w64[5];
     float w32[5];
     long long spin_limit;
+    int withhold;         // failure test: CTA 0 never raises its epoch flag, so its
+                          // neighbour's wait runs out (PCD_TIMEOUT); 0 in normal use
 };
 
 size_t persist_smem_bytes(int W, int H, int G, bool mixed);

@@ -20,6 +20,14 @@ Fixtures (all float64, seeded inputs, the reference run with max_threads=1):
   mesh resolution r (grid 4r): per-iteration step sizes, target areas, the
   first iteration's errors/raster, final phi / target points, and after the
   three height iterations h and the source points.
+* pipeline_r128.npz -- the same replay at the full-pipeline workload's own
+  size (mesh 128 x 128, 512 x 512 grids, width 0.5, focal length 1.5,
+  thickness 0.1, conv 0.01), kept compact: step sizes, target areas, the first
+  iteration's errors, the final target and source points (the vertex heights
+  are the source points' z) and the final h sampled every 4th cell.  About
+  five minutes of single-threaded CPU:
+
+      python tests/golden/make_golden.py --r128
 """
 from __future__ import annotations
 
@@ -118,6 +126,30 @@ def pipeline(R: O.Ref, res: int, seed: int, width=0.5, focal=1.5, thickness=0.1,
     return len(steps)
 
 
+def pipeline_compact(R: O.Ref, res: int, seed: int, width=0.5, focal=1.5, thickness=0.1, conv=0.01):
+    img = inputs.pipeline_image(res, seed)
+    d = O.RefDesign(R, res, res, 4 * res, 4 * res, width, width, focal, thickness, 1)
+    d.initialize(img)
+    out = {"params": np.array([res, width, focal, thickness, conv, seed]), "target_areas": d.get("target_areas")}
+    steps = []
+    for itr in range(50):
+        s = d.transport_iteration()
+        steps.append(s)
+        if itr == 0:
+            out["errors_0"] = d.get("errors")
+        if s < conv:
+            break
+    out["steps"] = np.array(steps)
+    out["target_points"] = d.get("target_points")
+    for itr in range(3):
+        d.height_iteration(itr)
+    out["h_sub4"] = np.ascontiguousarray(d.get("h")[::4, ::4])
+    out["source_points"] = d.get("source_points")
+    d.close()
+    np.savez_compressed(os.path.join(OUT, f"pipeline_r{res}.npz"), **out)
+    return len(steps)
+
+
 def writer_cases(R: O.Ref):
     import tempfile
 
@@ -169,6 +201,10 @@ def mesh_cases(R: O.Ref):
 def main():
     O.build(ref=True)
     R = O.Ref()
+    if "--r128" in sys.argv[1:]:
+        n = pipeline_compact(R, 128, 47)
+        print(f"pipeline r128: {n} transport iterations")
+        return
     solver_cases(R)
     utils_cases(R)
     writer_cases(R)

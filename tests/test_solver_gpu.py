@@ -415,3 +415,32 @@ def test_nan_cells_are_excluded_like_reference(ctx, port):
     assert np.array_equal(np.isnan(phi_gpu), np.isnan(phi_cpu))
     m = ~np.isnan(phi_cpu)
     assert _rel_mod_const(phi_gpu[m], phi_cpu[m])[0] < 1e-7
+
+
+def test_bounded_wait_runs_out_and_context_stays_usable(ctx):
+    """A device wait that runs out (failure handling without a GPU fault): the
+    persistent schedule's first CTA withholds its epoch flag, a flag nothing
+    else sets, with a 2000-poll limit on every wait.  Its neighbour's wait
+    gives up, records PCD_TIMEOUT, every CTA returns, and the solve reports
+    PCD_TIMEOUT (the reference's solver has no status at all,
+    solver.cpp:92-147).  The same context then solves normally."""
+    import poisson_caustic_design_gb300 as pcd
+
+    L = pcd._lib.load()
+    b = pcd.inputs.poisson_rhs(256, 6, "gaussian")
+    opts = pcd.SolveOptions(stop=pcd.STOP_REL_RESIDUAL, tol=1e-8, max_iterations=100000, omega=-1.0,
+                            schedule=pcd.SCHED_PERSISTENT)
+    assert L.pcd_ctx_set_wait_limit(ctx.handle, 2000, 1) == 0
+    try:
+        with pytest.raises(pcd.PCDError) as e:
+            ctx.solve(b, np.zeros_like(b), opts)
+        assert e.value.status == pcd._lib.PCD_TIMEOUT
+    finally:
+        assert L.pcd_ctx_set_wait_limit(ctx.handle, 0, 0) == 0
+    phi = np.zeros_like(b)
+    st = ctx.solve(b, phi, opts)
+    assert st["converged"] and st["schedule_used"] == pcd.SCHED_PERSISTENT
+    import oracle
+
+    assert _rel_mod_const(phi, oracle.dct_solve(b))[0] < 1e-6
+    assert L.pcd_ctx_set_wait_limit(ctx.handle, -1, 0) == pcd._lib.PCD_BAD_ARG

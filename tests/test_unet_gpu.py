@@ -239,3 +239,92 @@ def test_trained_network_gains_over_zero_guess(ctx):
         assert kept >= 3, (n, kept, ratios)
         assert np.mean(ratios) < 0.93, (n, ratios)
     net.close()
+
+
+def _trained_net(ctx):
+    from poisson_caustic_design_gb300 import learned
+
+    path = learned.default_weights_path(64)
+    if not os.path.exists(path):
+        pytest.skip("no trained weights in this checkout")
+    net = learned.UNet(ctx, resolution=64, max_batch=1)
+    net.load(path)
+    return net
+
+
+@pytest.mark.parametrize("seed", range(8))
+def test_headline_forms_on_bench_densities_vs_exact(ctx, seed):
+    """The single-solve workload's own eight densities (512 x 512, seeds 0-7,
+    Gaussian mixtures for even seeds and binary shapes for odd ones, b mean-free
+    in FP64) to relative residual 1e-6 with the Neumann-optimal omega: plain
+    FP64, FP32 sweeps + FP64 defect correction, and the learned warm start +
+    mixed.  Each form's residual, recomputed by the C port, is <= 1e-6 and its
+    error against the exact DCT solve (the FP64 oracle solved to ~1e-13) is
+    within 2x the plain FP64 form's + 1e-7, in L2 and max norm (mod const)."""
+    import torch
+
+    import oracle
+    import poisson_caustic_design_gb300 as pcd
+
+    kind = "gaussian" if seed % 2 == 0 else "binary"
+    b = pcd.inputs.poisson_rhs(512, seed, kind)
+    exact = oracle.dct_solve(b)
+    port = oracle.Port()
+    net = _trained_net(ctx)
+    net.attach(ctx)
+    bd = torch.from_numpy(b).cuda()
+    errs = {}
+    for name, prec, warm in (("plain", pcd.PREC_FP64, 0), ("mixed", pcd.PREC_MIXED, 0),
+                             ("learned", pcd.PREC_MIXED, 2)):
+        phi = torch.zeros_like(bd)
+        st = ctx.solve_device(bd, phi, pcd.SolveOptions(stop=pcd.STOP_REL_RESIDUAL, tol=1e-6, max_iterations=200000,
+                                                        precision=prec, omega=-1.0, warm_start=warm))
+        torch.cuda.synchronize()
+        assert st["converged"] and st["rel_residual"] <= 1e-6, (name, st)
+        p = phi.cpu().numpy()
+        _, rn, bn, _ = port.residual(b, p)
+        assert rn / bn <= 1.01e-6, (name, rn / bn)
+        errs[name] = oracle.rel_err_mod_const(p, exact)
+    for name in ("mixed", "learned"):
+        assert errs[name][0] <= 2 * errs["plain"][0] + 1e-7, errs
+        assert errs[name][1] <= 2 * errs["plain"][1] + 1e-7, errs
+    net.close()
+
+
+def test_forced_bad_prediction_falls_back_to_zero_guess(ctx):
+    """A network whose output is scaled by 1e3 (head weights and bias x 1e3)
+    predicts a potential far worse than a zero guess: the judge rejects it
+    (warm_used = 3, the zero-guess fallback) and the solve still reaches the
+    tolerance, to the same answer as a plain zero-guess mixed solve."""
+    import torch
+
+    import oracle
+    import poisson_caustic_design_gb300 as pcd
+    from poisson_caustic_design_gb300 import learned
+
+    net = _trained_net(ctx)
+    p = net.get_params()
+    layout, _ = learned.param_layout()
+    for name, off, shape in layout:
+        if name.startswith("head."):
+            p[off:off + int(np.prod(shape))] *= 1e3
+    net.set_params(p)
+    net.attach(ctx)
+    b = pcd.inputs.poisson_rhs(512, 900001, "binary")
+    bd = torch.from_numpy(b).cuda()
+    phi = torch.zeros_like(bd)
+    st = ctx.solve_device(bd, phi, pcd.SolveOptions(stop=pcd.STOP_REL_RESIDUAL, tol=1e-6, precision=pcd.PREC_MIXED,
+                                                    omega=-1.0, warm_start=2))
+    torch.cuda.synchronize()
+    assert st["warm_used"] == 3, st
+    assert st["warm_rel_residual"] > st["warm_zero_rel_residual"]
+    assert st["converged"] and st["rel_residual"] <= 1e-6
+    zero = torch.zeros_like(bd)
+    sz = ctx.solve_device(bd, zero, pcd.SolveOptions(stop=pcd.STOP_REL_RESIDUAL, tol=1e-6, precision=pcd.PREC_MIXED,
+                                                     omega=-1.0, warm_start=0))
+    torch.cuda.synchronize()
+    assert sz["sweeps"] == st["sweeps"]
+    e = oracle.rel_err_mod_const(phi.cpu().numpy(), zero.cpu().numpy())[0]
+    assert e < 1e-12, e
+    pcd._lib.load().pcd_ctx_set_warm_start_net(ctx.handle, None)
+    net.close()

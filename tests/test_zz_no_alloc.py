@@ -58,6 +58,37 @@ def test_noalloc_matches_existing_entry_point_twice():
     ctx.close()
 
 
+@pytest.mark.parametrize("h,w,fill", [
+    (16384, 8, "normal"),   # the largest accepted height: the scratch's last row slot
+    (4, 4, "nan"),          # every cell NaN: the 0/0 mean leaves every cell NaN, as utils.cpp:60-86 does
+    (3, 5000, "normal"),    # rows much wider than the 256-thread block (row-strided loop)
+])
+def test_noalloc_edges_match_existing_entry_point(h, w, fill):
+    import torch
+
+    import poisson_caustic_design_gb300 as pcd
+
+    L = _lib()
+    ctx = pcd.Context(0)
+    torch.cuda.set_device(0)
+    stream = torch.cuda.current_stream().cuda_stream
+    rng = np.random.default_rng(h * 7 + w)
+    a = np.full((h, w), np.nan) if fill == "nan" else rng.standard_normal((h, w)) + 2.5
+    ref = torch.from_numpy(a).cuda()
+    _run_existing(L, ctx, ref, w, h, stream)
+    for _ in range(2):   # two calls in a row on fresh copies of the same grid
+        o_t = torch.from_numpy(a).cuda()
+        st = L.pcd_subtract_average_noalloc(C.c_void_p(o_t.data_ptr()), w, h, C.c_void_p(stream))
+        assert st == 0, L.pcd_last_error().decode()
+        torch.cuda.synchronize()
+        r, o = ref.cpu().numpy(), o_t.cpu().numpy()
+        assert np.array_equal(np.isnan(r), np.isnan(o))
+        m = ~np.isnan(r)
+        if m.any():
+            np.testing.assert_allclose(o[m], r[m], rtol=0, atol=1e-12 * np.abs(a[m]).max())
+    ctx.close()
+
+
 def test_noalloc_rejects_grids_beyond_its_scratch():
     import torch
 
