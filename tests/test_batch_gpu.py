@@ -166,3 +166,28 @@ def test_batch_tile_form_padded_rows_and_sweep_cap(ctx):
         ref = single.cpu().numpy()
         err = np.abs(p.cpu().numpy() - ref).max() / np.abs(ref).max()
         assert err < 1e-6, ((w, h), err)
+
+
+def test_batch_tile_form_takes_short_and_wide_grids(ctx):
+    """The batched tile form has neither the cluster form's height floor
+    (2 x the cluster size) nor its 4096-column ceiling: a batch with a 16-row
+    grid and a 4104-column grid goes to the tile passes and every grid reaches
+    the tolerance against the exact solve."""
+    import torch
+
+    import oracle
+    import poisson_caustic_design_gb300 as pcd
+
+    shapes = [(64, 16), (4104, 40), (128, 128)]
+    rhs = [pcd.inputs.poisson_rhs(w, 70 + i, "gaussian", m=h) for i, (w, h) in enumerate(shapes)]
+    bs = [torch.from_numpy(b).cuda() for b in rhs]
+    phis = [torch.zeros_like(b) for b in bs]
+    opts = pcd.SolveOptions(stop=pcd.STOP_REL_RESIDUAL, tol=1e-8, max_iterations=400000, omega=-1.0,
+                            warm_start=False)
+    per, bst = pcd.batch_solve(ctx, bs, phis, opts)
+    torch.cuda.synchronize()
+    assert bst["status"] == 0 and bst["clusters"] == 0     # the tile form ran
+    for i, (b, p) in enumerate(zip(rhs, phis)):
+        assert per[i]["converged"] == 1, (shapes[i], per[i])
+        e2, _ = oracle.rel_err_mod_const(p.cpu().numpy(), oracle.dct_solve(b))
+        assert e2 < 1e-6, (shapes[i], e2)
