@@ -93,9 +93,20 @@ def test_batch_rejects_bad_instances(ctx):
 
     import poisson_caustic_design_gb300 as pcd
 
+    # 16 rows: below the cluster form's floor of 2 x 16 CTAs (the tile form,
+    # which takes such grids, is not used for a width that is not a multiple of 8)
+    b = torch.zeros((16, 18), dtype=torch.float64, device="cuda")
+    with pytest.raises(pcd.PCDError):
+        pcd.batch_solve(ctx, [b], [torch.zeros_like(b)])
+    # the same through the cluster form explicitly
     b = torch.zeros((16, 16), dtype=torch.float64, device="cuda")
     with pytest.raises(pcd.PCDError):
-        pcd.batch_solve(ctx, [b], [torch.zeros_like(b)])      # height < 32
+        pcd.batch_solve(ctx, [b], [torch.zeros_like(b)], pcd.SolveOptions(stop=pcd.STOP_REL_RESIDUAL, tol=1e-6,
+                                                                          schedule=pcd.SCHED_CLUSTER))
+    # the relative-residual stop is required
+    b = torch.zeros((64, 64), dtype=torch.float64, device="cuda")
+    with pytest.raises(pcd.PCDError):
+        pcd.batch_solve(ctx, [b], [torch.zeros_like(b)], pcd.SolveOptions(stop=pcd.STOP_MAX_UPDATE, tol=1e-6))
 
 
 TILE_SIZES = [(64, 64), (96, 64), (128, 128), (256, 200), (512, 512), (1024, 1024), (504, 33), (1024, 300)]
