@@ -79,6 +79,8 @@ typedef struct {
     double refine_drop;      /* mixed precision, cluster and batch schedules: an FP32 cycle ends
                                 once its residual estimate fell by this factor (then the FP64
                                 residual is refreshed); 0 = auto (3e-2) */
+    int block_sweeps;        /* block schedule: sweeps between halo exchanges, 1..8 (halo of
+                                2 x that many cells); 0 = auto (FP64 4, FP32 8) */
 } pcd_solve_opts;
 
 typedef enum {
@@ -111,7 +113,7 @@ typedef enum {
                                   stripe edges recomputed, no boundary pass); AUTO picks it for
                                   FP32 sweeps when neither the on-chip schedules nor the tile
                                   passes apply */
-    PCD_SCHED_TILES = 6        /* mixed precision, grids in HBM without NaN cells, width a multiple
+    PCD_SCHED_TILES = 6,       /* mixed precision, grids in HBM without NaN cells, width a multiple
                                   of 8, ld of 4: passes of up to 4 FP32 sweeps from one correction
                                   buffer into another, each tile of the grid held in registers
                                   for the whole pass (halo recomputed); check_every = sweeps per
@@ -119,6 +121,12 @@ typedef enum {
                                   stop may come up to 3 sweeps after the first passing sweep;
                                   AUTO picks it for FP32 sweeps when the cluster schedule does
                                   not apply */
+    PCD_SCHED_BLOCKS = 7       /* grids without NaN cells: one cooperative launch per solve on
+                                  2-D blocks (one per SM), each kept in shared memory with a
+                                  halo of 2K cells, K red-black sweeps between exchanges of
+                                  the halo rings through L2 (K = 2 FP64, 8 FP32); mixed
+                                  precision folds the FP32 correction into phi in FP64 inside
+                                  the launch.  Grids up to about a million cells */
 } pcd_schedule;
 
 typedef struct {

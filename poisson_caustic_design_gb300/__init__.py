@@ -11,7 +11,7 @@ the reference's interfaces:
 from . import inputs  # noqa: F401
 from ._lib import PCDError  # noqa: F401
 from .solver import (PREC_FP64, PREC_MIXED, SCHED_AUTO, SCHED_CLUSTER, SCHED_LAUNCHES,  # noqa: F401
-                     SCHED_PERSISTENT, SCHED_STREAM, SCHED_STRIPES, SCHED_TILES,
+                     SCHED_PERSISTENT, SCHED_STREAM, SCHED_STRIPES, SCHED_TILES, SCHED_BLOCKS,
                      STOP_MAX_UPDATE, STOP_REL_RESIDUAL, Context, SolveOptions, batch_solve, poisson_solver,
                      solver_progress)
 from .caustic_design import (CausticDesign, export_grid_to_svg, save_heightmap_as_json,  # noqa: F401

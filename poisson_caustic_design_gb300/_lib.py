@@ -36,6 +36,7 @@ SCHED_CLUSTER = 3
 SCHED_STRIPES = 4
 SCHED_STREAM = 5
 SCHED_TILES = 6
+SCHED_BLOCKS = 7
 WARM_ZERO = 0
 WARM_GIVEN = 1
 WARM_LEARNED = 2
@@ -59,6 +60,7 @@ class SolveOpts(C.Structure):
         ("warm_start", C.c_int),
         ("schedule", C.c_int),
         ("refine_drop", C.c_double),
+        ("block_sweeps", C.c_int),
     ]
 
 

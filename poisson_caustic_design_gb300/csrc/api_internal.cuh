@@ -16,6 +16,7 @@ namespace pcd {
 struct TunedSolve {
     int check_every = 0, refine_every = 0, schedule = PCD_SCHED_AUTO;
     double refine_drop = 0.0;
+    int block_sweeps = 0;
 };
 struct TunedBatch {
     int cluster = 16, check_every = 0;

@@ -48,12 +48,13 @@ long long bits(double d)
 std::vector<TunedSolve> solve_candidates(const pcd_solve_opts &o)
 {
     std::vector<TunedSolve> c;
-    auto add = [&](int ce, double drop, int re, int sched) {
+    auto add = [&](int ce, double drop, int re, int sched, int ks = 0) {
         TunedSolve t;
         t.check_every = ce;
         t.refine_drop = drop;
         t.refine_every = re;
         t.schedule = sched;
+        t.block_sweeps = ks;
         c.push_back(t);
     };
     if (o.precision == PCD_PREC_MIXED && o.stop == PCD_STOP_REL_RESIDUAL) {
@@ -69,7 +70,11 @@ std::vector<TunedSolve> solve_candidates(const pcd_solve_opts &o)
         for (int re : {32, 64, 128}) add(0, 0.0, re, PCD_SCHED_AUTO);
         add(0, 0.0, 0, PCD_SCHED_PERSISTENT);
     } else {
-        for (int ce : {8, 32}) add(ce, 0.0, 0, PCD_SCHED_AUTO);
+        // the block schedule with 2 or 4 sweeps per halo exchange (grids that
+        // fit on chip), the persistent bands, stripes and launches
+        for (int ks : {4, 2})
+            for (int ce : {16, 32}) add(ce, 0.0, 0, PCD_SCHED_BLOCKS, ks);
+        add(32, 0.0, 0, PCD_SCHED_PERSISTENT);
         add(32, 0.0, 0, PCD_SCHED_STRIPES);
         add(32, 0.0, 0, PCD_SCHED_LAUNCHES);
     }
@@ -82,6 +87,7 @@ pcd_solve_opts apply(pcd_solve_opts o, const TunedSolve &t)
     o.refine_every = t.refine_every;
     o.refine_drop = t.refine_drop;
     o.schedule = t.schedule;
+    o.block_sweeps = t.block_sweeps;
     return o;
 }
 
@@ -108,13 +114,14 @@ int solve_autotuned(pcd_ctx *ctx, const double *b, double *phi, int W, int H, in
 {
     Autotuner &T = ctx->tuner;
     const bool pinned = o.schedule != PCD_SCHED_AUTO || o.check_every != 0 || o.refine_every != 0 ||
-                        o.refine_drop != 0.0;
+                        o.refine_drop != 0.0 || o.block_sweeps != 0;
     if (!T.enabled || pinned) {
         TunedSolve given;
         given.check_every = o.check_every;
         given.refine_every = o.refine_every;
         given.refine_drop = o.refine_drop;
         given.schedule = o.schedule;
+        given.block_sweeps = o.block_sweeps;
         const int st = solve_device(ctx->solver, b, phi, W, H, ld, o, stats, s);
         note(stats, given, 0);
         return st;

@@ -30,6 +30,7 @@
 #include "solver.cuh"
 #include "sor_persist.cuh"
 #include "sor_cluster.cuh"
+#include "sor_blocks.cuh"
 
 namespace pcd {
 
@@ -599,8 +600,9 @@ void SolverWorkspace::release()
     if (xbuf) cudaFree(xbuf);
     if (flags) cudaFree(flags);
     if (part) cudaFree(part);
-    r64 = nullptr; xbuf = nullptr; flags = nullptr; part = nullptr;
-    xbuf_elems = 0; max_ctas = 0;
+    if (bx) cudaFree(bx);
+    r64 = nullptr; xbuf = nullptr; flags = nullptr; part = nullptr; bx = nullptr;
+    xbuf_elems = 0; max_ctas = 0; bx_bytes = 0;
     if (partials) cudaFree(partials);
     if (ctl) cudaFree(ctl);
     if (ctl_host) cudaFreeHost(ctl_host);
@@ -863,6 +865,97 @@ int solve_persistent(SolverWorkspace &ws, const double *b, double *phi, const So
     return converged ? PCD_OK : PCD_NOT_CONVERGED;
 }
 
+// The CTA-count dependent buffers of the persistent schedules: G epoch flags
+// plus a barrier counter, and 2 x G x 3 check partials.
+int reserve_ctas(SolverWorkspace &ws, int G)
+{
+    if (G > ws.max_ctas) {
+        if (ws.flags) cudaFree(ws.flags);
+        if (ws.part) cudaFree(ws.part);
+        ws.flags = nullptr;
+        ws.part = nullptr;
+        ws.max_ctas = 0;
+        PCD_CUDA(cudaMalloc(&ws.flags, (G + 1) * sizeof(unsigned)));
+        PCD_CUDA(cudaMalloc(&ws.part, 2 * 3 * G * sizeof(double)));
+        ws.max_ctas = G;
+    }
+    return PCD_OK;
+}
+
+// One cooperative launch per solve on 2-D blocks with deep halos
+// (sor_blocks.cu), then the exact FP64 statistics of the returned phi.
+int solve_blocks(SolverWorkspace &ws, const double *b, double *phi, const SolveArgs &a, int precision,
+                 const pcd_solve_opts &o, const BlocksPlan &bp, pcd_solve_stats *stats, cudaStream_t s)
+{
+    const bool mixed = precision == PCD_PREC_MIXED;
+    const int G = bp.TY * bp.TX;
+    const int xs = (a.W + 3) & ~3;
+    const size_t elt = mixed ? sizeof(float) : sizeof(double);
+    const size_t need = 2 * (size_t)a.H * xs * elt + (mixed ? (size_t)a.H * xs * sizeof(float) : 0);
+    if (need > ws.bx_bytes) {
+        if (ws.bx) cudaFree(ws.bx);
+        ws.bx = nullptr;
+        ws.bx_bytes = 0;
+        PCD_CUDA(cudaMalloc(&ws.bx, need));
+        ws.bx_bytes = need;
+    }
+    PCD_TRY(reserve_ctas(ws, G));
+    PCD_CUDA(cudaMemsetAsync(ws.flags, 0, (G + 1) * sizeof(unsigned), s));
+
+    BlocksArgs ba{};
+    ba.W = a.W; ba.H = a.H; ba.ld = a.ld;
+    ba.TY = bp.TY; ba.TX = bp.TX; ba.G = G; ba.K = bp.K; ba.RTmax = bp.RTmax; ba.xs = xs;
+    ba.b = b; ba.phi = phi; ba.r64 = ws.r64;
+    ba.xb = ws.bx;
+    ba.r32x = mixed ? reinterpret_cast<float *>(static_cast<char *>(ws.bx) + 2 * (size_t)a.H * xs * elt) : nullptr;
+    ba.flags = ws.flags; ba.part = ws.part; ba.ctl = ws.ctl;
+    ba.stop = a.stop; ba.max_iter = a.max_iter; ba.tol = a.tol; ba.omega = a.omega;
+    // a stop test costs a grid barrier (a few L2 round trips): every 16
+    // sweeps for the max-update stop, 32 for the relative residual
+    int ce = o.check_every > 0 ? o.check_every : (a.stop == PCD_STOP_MAX_UPDATE ? 16 : 32);
+    ce = std::max(bp.K, (ce + bp.K - 1) / bp.K * bp.K);  // a multiple of the sweeps per exchange
+    ba.check_every = ce;
+    ba.cycle_cap = o.refine_every > 0 ? o.refine_every : 2048;
+    ba.drop = o.refine_drop > 0.0 ? o.refine_drop : 3e-2;
+    for (int c = 0; c < 5; c++) { ba.w64[c] = a.w64[c]; ba.w32[c] = a.w32[c]; }
+    ba.spin_limit = ws.wait_limit > 0 ? ws.wait_limit : 1ll << 24;
+    ba.withhold = ws.withhold_flag;
+    PCD_CUDA(cudaEventRecord(ws.k0, s));
+    PCD_TRY(launch_blocks(ba, mixed, bp.smem, s));
+    PCD_CUDA(cudaEventRecord(ws.k1, s));
+
+    // exact FP64 statistics of the returned phi
+    const int rblocks = grid_blocks((long)a.W * a.H);
+    k_residual64<false><<<rblocks, kThreads, 0, s>>>(phi, b, ws.mask, ws.ctl, ws.partials, a, 0, 1, 0);
+    PCD_LAUNCHED(1);
+    PCD_CUDA(cudaEventRecord(ws.t1, s));
+    PCD_CUDA(cudaMemcpyAsync(&ws.ctl_host[0], ws.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, s));
+    PCD_CUDA(cudaStreamSynchronize(s));
+    const Ctl &c = ws.ctl_host[0];
+    if (c.error) {
+        set_error("block SOR: a bounded device wait gave up (status " + std::to_string(c.error) + ")");
+        return c.error;
+    }
+    int converged = c.converged;
+    if (a.stop == PCD_STOP_REL_RESIDUAL) converged = c.rel <= a.tol;
+    if (stats) {
+        stats->sweeps = c.sweeps;
+        stats->converged = converged;
+        stats->rel_residual = c.rel;
+        stats->max_residual = c.rmax;
+        stats->last_max_update = c.last_max;
+        stats->residual_checks = c.checks + 2;
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, ws.t0, ws.t1);
+        stats->device_ms = ms;
+        cudaEventElapsedTime(&ms, ws.k0, ws.k1);
+        stats->sweep_ms = ms;
+        stats->schedule_used = PCD_SCHED_BLOCKS;
+        stats->check_every_used = ce;
+    }
+    return converged ? PCD_OK : PCD_NOT_CONVERGED;
+}
+
 }  // namespace
 
 namespace {
@@ -1055,6 +1148,25 @@ int solve_device(SolverWorkspace &ws, const double *b, double *phi, int W, int H
     const int masked = ws.ctl_host[0].nan_cells > 0 ? 1 : 0;
     const bool done_already = ws.ctl_host[0].converged != 0 || a.max_iter == 0;
 
+    // FP64 sweeps: the block schedule (on chip, 2-D blocks, one L2 exchange per
+    // K sweeps) before the persistent bands (one per half sweep): 6.4 against
+    // 16.0 us per 512^2 sweep, 17 against 28 us (stripes) at 1024^2
+    const bool auto_blocks = o.schedule == PCD_SCHED_AUTO && precision == PCD_PREC_FP64 &&
+                             (long)W * H >= kTileMinCells;
+    if (!done_already && !masked && (o.schedule == PCD_SCHED_BLOCKS || auto_blocks)) {
+        BlocksPlan bp{};
+        const bool mixed = precision == PCD_PREC_MIXED;
+        int st = PCD_BAD_ARG;
+        if (o.block_sweeps < 0 || o.block_sweeps > 8) {
+            set_error("pcd solve: block_sweeps must be 0 (auto) or 1..8");
+            return PCD_BAD_ARG;
+        }
+        if (o.block_sweeps > 0) st = blocks_plan(ws.dev, W, H, o.block_sweeps, mixed, &bp);
+        else
+            for (int K : {mixed ? 8 : 4, 4, 2, 1})
+                if ((st = blocks_plan(ws.dev, W, H, K, mixed, &bp)) == PCD_OK) break;
+        if (st == PCD_OK) return solve_blocks(ws, b, phi, a, precision, o, bp, stats, s);
+    }
     if (!done_already && !masked && precision == PCD_PREC_MIXED && a.stop == PCD_STOP_REL_RESIDUAL &&
         (o.schedule == PCD_SCHED_AUTO || o.schedule == PCD_SCHED_CLUSTER)) {
         ClusterPlan plan{};

@@ -100,6 +100,9 @@ struct SolverWorkspace {
     // up (0: 2^24), and the failure test's withheld flag (pcd_ctx_set_wait_limit)
     long long wait_limit = 0;
     int withhold_flag = 0;
+    // the block schedule's exchange grids (and the mixed form's FP32 rhs grid)
+    void *bx = nullptr;
+    size_t bx_bytes = 0;
 
     struct GraphEntry {
         cudaGraphExec_t exec;

@@ -20,12 +20,12 @@ import numpy as np
 
 from . import _lib
 from ._lib import (PREC_FP64, PREC_MIXED, SCHED_AUTO, SCHED_CLUSTER, SCHED_LAUNCHES, SCHED_PERSISTENT, SCHED_STREAM,
-                   SCHED_STRIPES, SCHED_TILES, STOP_MAX_UPDATE,
+                   SCHED_STRIPES, SCHED_TILES, SCHED_BLOCKS, STOP_MAX_UPDATE,
                    STOP_REL_RESIDUAL, check)
 
 __all__ = ["poisson_solver", "batch_solve", "solver_progress", "Context", "SolveOptions", "PREC_FP64", "PREC_MIXED",
            "STOP_MAX_UPDATE", "STOP_REL_RESIDUAL", "SCHED_AUTO", "SCHED_LAUNCHES", "SCHED_PERSISTENT",
-           "SCHED_CLUSTER", "SCHED_STRIPES", "SCHED_STREAM", "SCHED_TILES"]
+           "SCHED_CLUSTER", "SCHED_STRIPES", "SCHED_STREAM", "SCHED_TILES", "SCHED_BLOCKS"]
 
 # solver.h:10 declares `extern double solver_progress`; the reference never
 # updates it (solver.cpp:9,63-68), so neither does this mirror.
@@ -44,6 +44,7 @@ class SolveOptions:
     warm_start: int = 1      # 0 zero, 1 phi is the initial guess, 2 learned prediction
     schedule: int = 0
     refine_drop: float = 0.0
+    block_sweeps: int = 0
 
     def to_c(self) -> _lib.SolveOpts:
         o = _lib.SolveOpts()
@@ -57,6 +58,7 @@ class SolveOptions:
         o.warm_start = int(self.warm_start)
         o.schedule = int(self.schedule)
         o.refine_drop = float(self.refine_drop)
+        o.block_sweeps = int(self.block_sweeps)
         return o
 
 

@@ -444,3 +444,74 @@ def test_bounded_wait_runs_out_and_context_stays_usable(ctx):
 
     assert _rel_mod_const(phi, oracle.dct_solve(b))[0] < 1e-6
     assert L.pcd_ctx_set_wait_limit(ctx.handle, -1, 0) == pcd._lib.PCD_BAD_ARG
+
+
+@pytest.mark.parametrize("n,m", [(512, 512), (96, 80), (33, 17), (1024, 700), (200, 1000), (64, 64), (9, 1000)])
+@pytest.mark.parametrize("prec", [0, 1])
+def test_block_schedule_matches_launch_schedule(ctx, n, m, prec):
+    """The block schedule (2-D blocks with halos of 2K cells, K sweeps between
+    halo exchanges, K = 2 in FP64 and up to 8 in FP32) runs the same red-black
+    iteration as one launch per half sweep: after the same number of sweeps,
+    37 (not a multiple of K, so the last pass is shorter), the iterates agree
+    to rounding (FP64: 1e-11 of the field's scale; the mixed form, with the
+    FP32 correction folded into phi every 16 sweeps by both schedules: FP32
+    rounding, 1e-5).  A wrong halo or dependency cone would show as an O(1)
+    difference at the block edges."""
+    import poisson_caustic_design_gb300 as pcd
+
+    b = pcd.inputs.poisson_rhs(n, 8, "binary" if n % 2 else "gaussian", m=m)
+    out = {}
+    for sched in (pcd.SCHED_LAUNCHES, pcd.SCHED_BLOCKS):
+        phi = np.zeros_like(b)
+        st = ctx.solve(b, phi, pcd.SolveOptions(stop=pcd.STOP_REL_RESIDUAL, tol=0.0, max_iterations=37,
+                                                schedule=sched, omega=-1.0, precision=prec, refine_every=16,
+                                                check_every=16))
+        assert st["sweeps"] == 37 and st["schedule_used"] == sched, st
+        out[sched] = phi
+    a, c = out[pcd.SCHED_LAUNCHES], out[pcd.SCHED_BLOCKS]
+    tol = 1e-11 if prec == 0 else 1e-5
+    assert np.abs(a - c).max() <= tol * np.abs(a).max(), np.abs(a - c).max() / np.abs(a).max()
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+@pytest.mark.parametrize("stop,tol", [(1, 1e-9), (0, 1e-9)])
+@pytest.mark.parametrize("n,m", [(512, 512), (256, 256), (640, 480), (33, 17)])
+def test_block_schedule_reaches_exact_solve(ctx, n, m, prec, stop, tol):
+    """Both stop tests on the block schedule, FP64 and mixed: converged, and
+    within 1e-6 of the exact DCT solve (relative L2, mod the constant); the
+    relative-residual stop's reported residual is the oracle's."""
+    import oracle
+    import poisson_caustic_design_gb300 as pcd
+
+    b = pcd.inputs.poisson_rhs(n, 9, "gaussian", m=m)
+    phi = np.zeros_like(b)
+    st = ctx.solve(b, phi, pcd.SolveOptions(stop=stop, tol=tol, max_iterations=200000, schedule=pcd.SCHED_BLOCKS,
+                                            omega=-1.0, precision=prec))
+    assert st["converged"] and st["schedule_used"] == pcd.SCHED_BLOCKS, st
+    assert _rel_mod_const(phi, oracle.dct_solve(b))[0] < 1e-6
+    _, rn, bn, _ = oracle.Port().residual(b, phi)
+    assert abs(rn / bn - st["rel_residual"]) <= 1e-3 * st["rel_residual"] + 1e-15
+    if stop == 1:
+        assert rn / bn <= tol * 1.0001
+
+
+def test_block_schedule_wait_runs_out(ctx):
+    """The block schedule's flag waits are bounded like the persistent
+    schedule's: with the first block's epoch flag withheld the solve returns
+    PCD_TIMEOUT, and the context solves normally afterwards."""
+    import poisson_caustic_design_gb300 as pcd
+
+    L = pcd._lib.load()
+    b = pcd.inputs.poisson_rhs(256, 10, "binary")
+    opts = pcd.SolveOptions(stop=pcd.STOP_REL_RESIDUAL, tol=1e-8, max_iterations=100000, omega=-1.0,
+                            schedule=pcd.SCHED_BLOCKS)
+    assert L.pcd_ctx_set_wait_limit(ctx.handle, 2000, 1) == 0
+    try:
+        with pytest.raises(pcd.PCDError) as e:
+            ctx.solve(b, np.zeros_like(b), opts)
+        assert e.value.status == pcd._lib.PCD_TIMEOUT
+    finally:
+        assert L.pcd_ctx_set_wait_limit(ctx.handle, 0, 0) == 0
+    phi = np.zeros_like(b)
+    st = ctx.solve(b, phi, opts)
+    assert st["converged"] and st["schedule_used"] == pcd.SCHED_BLOCKS
