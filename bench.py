@@ -41,6 +41,13 @@ TOL = 1e-6
 METRIC = "OT solve wall-time to residual 1e-6 at 512²: learned+mixed vs plain GPU"
 UNIT = "ms/solve"
 SEEDS = [(s, "gaussian" if s % 2 == 0 else "binary") for s in range(8)]
+# DRAM bytes (read + write) of one k_sor_cluster_rr launch of the autotuned
+# headline solve, ncu (profiles/k_sor_cluster_rr_512_autotuned.md)
+CLUSTER_DRAM_BYTES_PER_LAUNCH = 2.164992e6
+# FP64 operations per cell-sweep of the block schedule's update and the
+# measured FP64 FMA rate of this part (dependent-free FMA loop, all SMs)
+FP64_OPS_PER_CELL = 5
+FP64_OPS_PER_S = 0.60e12
 
 
 def parse():
@@ -63,6 +70,11 @@ def parse():
     ap.add_argument("--config4", action="store_true",
                     help="instead of the headline: the full caustic pipeline at a 1024^2 mesh on 4096^2 grids "
                          "(transport and height iterations, plain FP64 and mixed), one JSON line")
+    ap.add_argument("--cpu-sample", type=float, default=None, metavar="BUDGET_S",
+                    help="internal: time the reference's CPU solver on the eight densities in this fresh process "
+                         "(per-solve budget BUDGET_S) and print one JSON object")
+    ap.add_argument("--cpu-omega", choices=["reference", "neumann"], default="reference",
+                    help="internal, with --cpu-sample: the reference's omega or the Neumann-optimal one")
     return ap.parse_args()
 
 
@@ -154,20 +166,52 @@ def instances():
 
 
 # ---------------------------------------------------------------------------
-def cpu_reference_solve(port, b, threads, budget_s, chunk=25):
+def exact_solve(b):
+    """The FP64 solution of the reference operator (Neumann graph Laplacian,
+    solver.cpp:29-47) to machine precision: DCT-II diagonalisation with the
+    eigenvalues 2 cos(pi k / W) + 2 cos(pi l / H) - 4, mean-zero (the accuracy
+    yardstick of every timed form, computed on the host outside the timed
+    region)."""
+    from scipy.fft import dctn, idctn
+
+    h, w = b.shape
+    bh = dctn(b - b.mean(), type=2, norm="ortho")
+    lam = (2.0 * np.cos(np.pi * np.arange(h) / h) - 2.0)[:, None] + (2.0 * np.cos(np.pi * np.arange(w) / w) - 2.0)
+    lam[0, 0] = 1.0
+    ph = bh / lam
+    ph[0, 0] = 0.0
+    return idctn(ph, type=2, norm="ortho")
+
+
+def err_mod_const(x, ref):
+    """(relative L2, relative max) error of x against ref, both mean-removed."""
+    x = x - x.mean()
+    ref = ref - ref.mean()
+    d = x - ref
+    return float(np.linalg.norm(d) / np.linalg.norm(ref)), float(np.abs(d).max() / np.abs(ref).max())
+
+
+def neumann_omega(n):
+    """The optimal SOR factor of the Neumann operator on an n x n grid (the
+    GPU forms' omega): 2 / (1 + sin t) with cos t = (1 + cos(pi / n)) / 2."""
+    mu = 0.5 * (1.0 + np.cos(np.pi / n))
+    return 2.0 / (1.0 + np.sqrt(1.0 - mu * mu))
+
+
+def cpu_reference_solve(port, b, threads, budget_s, chunk=25, omega=0.0):
     """The reference's solver on the host: chunks of `chunk` sweeps of its
     tile-threaded SOR (poisson_solver(b, phi, W, H, chunk, 0.0, T) warm-started
-    in place), relative residual checked between chunks outside the timed
-    region.  Returns (ms to tolerance or extrapolated, sweeps, rel, extrapolated)."""
+    in place; omega 0 = the reference's 2/(1+pi/W)), relative residual checked
+    between chunks outside the timed region.  Returns (ms to tolerance or
+    extrapolated, sweeps, rel, extrapolated)."""
     phi = np.zeros_like(b)
     t_solve = 0.0
     sweeps = 0
-    rel0 = 1.0
     rel = 1.0
     hist = []
     while True:
         t = time.perf_counter()
-        port.poisson_solver_threads(b, phi, chunk, 0.0, threads)
+        port.poisson_solver_threads(b, phi, chunk, 0.0, threads, omega)
         t_solve += time.perf_counter() - t
         sweeps += chunk
         _, rn, bn, _ = port.residual(b, phi)
@@ -182,6 +226,40 @@ def cpu_reference_solve(port, b, threads, budget_s, chunk=25):
             more = (np.log(TOL) - np.log(r1)) / rate if rate < 0 else float("inf")
             per_sweep = (t1 - t0) / (s1 - s0)
             return (t_solve + more * per_sweep) * 1e3, sweeps + int(more), rel, True
+
+
+def cpu_sample(budget_s, omega_kind="reference", seeds=None):
+    """The reference's threaded CPU solver on the workload's densities (all
+    eight by default), one solve each, in the calling process: mean ms per
+    solve, sweeps per solve, and whether a solve was extrapolated."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+
+    oracle.build(ref=False)
+    port = oracle.Port()
+    threads = os.cpu_count() or 1
+    seg = int(np.floor(np.sqrt(threads)))
+    omega = neumann_omega(N_GRID) if omega_kind == "neumann" else 0.0
+    bs = instances()
+    per = []
+    for k in (seeds if seeds is not None else range(len(bs))):
+        ms, sweeps, rel, ex = cpu_reference_solve(port, bs[k], threads, budget_s, omega=omega)
+        per.append({"seed": SEEDS[k][0], "kind": SEEDS[k][1], "ms": ms, "sweeps": sweeps, "extrapolated": ex})
+    return {"ms": float(np.mean([p["ms"] for p in per])), "sweeps": float(np.mean([p["sweeps"] for p in per])),
+            "extrapolated": any(p["extrapolated"] for p in per), "threads": seg * seg, "omega": omega_kind,
+            "per_solve": per}
+
+
+def cpu_sample_subprocess(budget_s, omega_kind="reference"):
+    """cpu_sample in a fresh interpreter: no CUDA context and no runtime
+    threads of this process compete with the solver's fork-join threads."""
+    env = {**os.environ, "WORLD_SIZE": "1", "RANK": "0"}
+    r = subprocess.run([sys.executable, os.path.abspath(__file__), "--cpu-sample", str(budget_s), "--cpu-omega",
+                        omega_kind], capture_output=True, text=True, env=env)
+    lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
+    if r.returncode != 0 or not lines:
+        raise RuntimeError(f"CPU baseline subprocess failed ({r.returncode}): {r.stderr[-500:]}")
+    return json.loads(lines[-1])
 
 
 def run_reference(args, rank, world, pg):
@@ -199,12 +277,16 @@ def run_reference(args, rank, world, pg):
     budget = max(2.0, min(args.cpu_budget_s, 150.0 / max(1, args.steps + args.warmup)))
     for w in range(args.warmup):
         cpu_reference_solve(port, bs[w % len(bs)], threads, budget)
-    times, extrap = [], False
+    times, sweeps_l, extrap = [], [], False
     for k in range(args.steps):
         ms, sweeps, rel, ex = cpu_reference_solve(port, bs[k % len(bs)], threads, budget)
         times.append(ms)
+        sweeps_l.append(sweeps)
         extrap |= ex
     v = float(np.mean(times))
+    # the same solver with the Neumann-optimal omega that the GPU forms use:
+    # splits the GPU/CPU ratio into the omega (algorithm) and the hardware
+    neu = cpu_sample(budget, "neumann")
     sample = (f"{args.steps} solves of 512x512 (Gaussian/binary RHS) to rel residual 1e-6, tile-threaded "
               f"lexicographic SOR with the reference's omega on {seg * seg} tile threads; chunks of 25 sweeps, "
               f"residual checks outside the timed region" + ("; slow solves extrapolated from the chunk rate"
@@ -217,6 +299,11 @@ def run_reference(args, rank, world, pg):
                    "tol": TOL, "l2": "host CPU run"},
         "cpu_baseline": {"value": v, "unit": UNIT, "cores": seg * seg, "kind": "port", "sample": sample},
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "sweeps_per_solve": float(np.mean(sweeps_l)),
+        "neumann_omega_variant": {"ms_per_solve": neu["ms"], "sweeps_per_solve": neu["sweeps"],
+                                  "extrapolated": neu["extrapolated"],
+                                  "note": "the same CPU solver on the eight densities with the Neumann-optimal "
+                                          "omega of the GPU forms (not the reference's own omega)"},
     }
     print(json.dumps(line), flush=True)
 
@@ -345,7 +432,7 @@ def run_ours(args, rank, world, local, pg):
         barrier(pg)
         if name == headline:
             launches_before = L.pcd_kernel_launches()
-        ms, sweeps, sweep_ms, rels, warm = [], [], [], [], []
+        ms, sweeps, sweep_ms, rels, warm, checks = [], [], [], [], [], []
         for k in range(args.steps):
             t, st = timed(opts, k)
             ms.append(t)
@@ -353,12 +440,14 @@ def run_ours(args, rank, world, local, pg):
             sweep_ms.append(st["sweep_ms"])
             rels.append(st["rel_residual"])
             warm.append(st["warm_used"])
+            checks.append(st["residual_checks"])
         torch.cuda.synchronize()
         barrier(pg)
         if name == headline:
             launches = L.pcd_kernel_launches() - launches_before
         results[name] = {"ms": max_over_ranks(pg, float(np.sum(ms))) / args.steps, "sweeps": float(np.mean(sweeps)),
                          "sweep_ms": float(np.mean(sweep_ms)), "max_rel_residual": float(np.max(rels)),
+                         "residual_checks": float(np.mean(checks)),
                          "schedule": int(st["schedule_used"]),
                          "tuned": {"check_every": st["check_every_used"], "refine_every": st["refine_every_used"],
                                    "refine_drop": st["refine_drop_used"]}}
@@ -367,19 +456,19 @@ def run_ours(args, rank, world, local, pg):
 
     acc, e2e, e2e_ms = {}, None, []
     if not args.headline_only:
-        # accuracy against an FP64 solve to 1e-12 (the plain FP64 solver, itself
-        # checked against the exact DCT solve in the tests) -- outside timing
-        b0 = bs[0]
-        ref = torch.zeros_like(phi)
-        ctx.solve_device(b0, ref, pcd.SolveOptions(stop=pcd.STOP_REL_RESIDUAL, tol=1e-12, max_iterations=400000,
-                                                   omega=-1.0, warm_start=False), stream=stream.cuda_stream)
+        # accuracy of every form on every one of the eight densities against
+        # the exact FP64 solve (DCT, residual ~1e-13), outside the timed region
+        exact = [exact_solve(b) for b in bs_host]
         for name, opts in forms.items():
-            out = torch.zeros_like(phi)
-            ctx.solve_device(b0, out, opts, stream=stream.cuda_stream)
-            torch.cuda.synchronize()
-            d = (out - out.mean()) - (ref - ref.mean())
-            r = ref - ref.mean()
-            acc[name] = {"l2": float(d.norm() / r.norm()), "max": float(d.abs().max() / r.abs().max())}
+            per = []
+            for k, b in enumerate(bs):
+                out = torch.zeros_like(phi)
+                ctx.solve_device(b, out, opts, stream=stream.cuda_stream)
+                torch.cuda.synchronize()
+                per.append(err_mod_const(out.cpu().numpy(), exact[k]))
+            acc[name] = {"l2_mean": float(np.mean([p[0] for p in per])), "l2_max": float(max(p[0] for p in per)),
+                         "max_mean": float(np.mean([p[1] for p in per])), "max_max": float(max(p[1] for p in per)),
+                         "instances": len(per), "reference": "exact FP64 DCT solve of the same b"}
 
         # end to end through the host-array C ABI: pinned b in, phi out
         hopts = forms[headline]
@@ -401,25 +490,37 @@ def run_ours(args, rank, world, local, pg):
         print("e2e samples (ms): " + " ".join(f"{t:.2f}" for t in e2e_ms), file=sys.stderr, flush=True)
 
     # roofline of the dominant kernel of the headline step: the FP32 cluster
-    # sweep kernel (k_sor_cluster_rr).  Algorithmic bytes per cell-sweep: 12
-    # (read e, read r32, write e in FP32), over the sweep kernels' device time
-    # (CUDA events on the context stream around the cycle loop).
+    # sweep kernel (k_sor_cluster_rr, one launch per FP32 cycle).  Algorithmic
+    # bytes per cell-sweep: 12 (read e, read r32, write e in FP32); a launch
+    # runs sweeps / cycles sweeps (cycles = FP64 residual evaluations - 1 on
+    # the cluster schedule), over the sweep kernels' device time (CUDA events
+    # on the context stream around the cycle loop).
     hm = results[headline]
     cells = N_GRID * N_GRID
     alg_bytes = 12.0 * cells * hm["sweeps"]
     achieved = alg_bytes / (hm["sweep_ms"] * 1e-3) / 1e9
     peak, peak_src = measured_hbm_peak()
-    # DRAM bytes of one k_sor_cluster_rr launch (one FP32 cycle, ~430 sweeps
-    # at 512^2) from the ncu capture summarised in
-    # profiles/k_sor_cluster_rr_512_full.md: the band load of e and r32 (the
-    # store stays in L2), against ~1.35 GB of algorithmic bytes per launch
+    cycles = max(1.0, hm["residual_checks"] - 1.0)
+    # DRAM bytes per k_sor_cluster_rr launch of the autotuned headline
+    # configuration, from one ncu capture: the band load of e and r32 only --
+    # the grid stays on the cluster for the whole launch
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-            "traffic": 2.164992e6, "traffic_unit": "bytes per launch (ncu)",
-            "alg_bytes_per_launch": 12.0 * cells * 430, "peak_source": peak_src,
-            "kernel": "k_sor_cluster_rr (FP32 sweeps)", "alg_bytes_per_solve": alg_bytes,
+            "traffic": CLUSTER_DRAM_BYTES_PER_LAUNCH, "traffic_unit": "bytes per launch (ncu)",
+            "alg_bytes_per_launch": alg_bytes / cycles, "sweeps_per_launch": hm["sweeps"] / cycles,
+            "peak_source": peak_src, "kernel": "k_sor_cluster_rr (FP32 sweeps)", "alg_bytes_per_solve": alg_bytes,
             "note": "the 512^2 working set stays on one 16-CTA cluster for a whole FP32 cycle (e in registers, "
                     "r32 in shared memory): the kernel is bound by FP32 issue, block and cluster barriers, not "
                     "HBM; DRAM traffic per launch is the band load and store (ncu summary under profiles/)"}
+    # the plain FP64 form's sweep kernel (the block schedule at 512^2) is bound
+    # by the FP64 pipe: reported against the measured FP64 FMA rate of this part
+    if "plain_fp64" in results:
+        pf = results["plain_fp64"]
+        us = 1e3 * pf["sweep_ms"] / max(1.0, pf["sweeps"])
+        roof["plain_fp64_sweep"] = {"us_per_sweep": us, "schedule": pf["schedule"],
+                                    "alg_gbs": 24.0 * cells / (us * 1e-6) / 1e9,
+                                    "fp64_issue_bound_us": FP64_OPS_PER_CELL * cells / FP64_OPS_PER_S * 1e6,
+                                    "note": "5 FP64 operations per cell-sweep over the measured 0.60 TFMA/s "
+                                            "FP64 rate of this part"}
 
     # batched configuration: 64 instances, sizes uniform in {64..1024}^2,
     # batched tile passes or the cluster form (CUDA graphs, the autotuner
@@ -457,18 +558,18 @@ def run_ours(args, rank, world, local, pg):
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline and not args.headline_only:
-        sys.path.insert(0, os.path.join(ROOT, "oracle"))
-        import oracle
-
-        oracle.build(ref=False)
-        port = oracle.Port()
-        threads = os.cpu_count() or 1
-        seg = int(np.floor(np.sqrt(threads)))
-        cms, csw, crel, cex = cpu_reference_solve(port, bs_host[0], threads, args.cpu_budget_s)
-        cpu = {"value": cms, "unit": UNIT, "cores": seg * seg, "kind": "port",
-               "sample": (f"one 512x512 Gaussian-RHS solve to rel residual 1e-6 ({csw} sweeps"
-                          + (", extrapolated from the chunk rate" if cex else "") + ") of the reference's "
-                          f"tile-threaded SOR schedule on {seg * seg} threads")}
+        # the reference's threaded solver on the same eight densities as the
+        # reference arm, in a fresh process (no CUDA context, no runtime threads
+        # of this one competing with its fork-join threads), 3 s per solve at
+        # most (slower solves extrapolated from their chunk rate)
+        cs = cpu_sample_subprocess(3.0)
+        cpu = {"value": cs["ms"], "unit": UNIT, "cores": cs["threads"], "kind": "port",
+               "sweeps_per_solve": cs["sweeps"],
+               "sample": (f"one solve of each of the eight 512x512 densities (Gaussian/binary) to rel residual 1e-6 "
+                          f"({cs['sweeps']:.0f} sweeps on average" + (", slow solves extrapolated from the chunk "
+                                                                       "rate" if cs["extrapolated"] else "")
+                          + f") of the reference's tile-threaded SOR schedule on {cs['threads']} threads, in a "
+                          "separate process")}
 
     line = {
         "metric": METRIC, "value": hm["ms"], "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -482,7 +583,7 @@ def run_ours(args, rank, world, local, pg):
                    "autotuned": not args.no_autotune,
                    "schedule": {1: "launches", 2: "persistent", 3: "cluster", 4: "stripes",
                                 5: "stream"}.get(hm["schedule"], "?")},
-        "forms": {k: {**v, "err_vs_fp64_1e-12": acc.get(k)} for k, v in results.items()},
+        "forms": {k: {**v, "err_vs_exact_fp64": acc.get(k)} for k, v in results.items()},
         "speedup_plain_over_mixed": (results["plain_fp64"]["ms"] / results["mixed"]["ms"]
                                      if "plain_fp64" in results else None),
         "speedup_plain_over_headline": (results["plain_fp64"]["ms"] / hm["ms"] if "plain_fp64" in results else None),
@@ -574,6 +675,9 @@ def run_config4(args, local):
 
 def main():
     args = parse()
+    if args.cpu_sample is not None:
+        print(json.dumps(cpu_sample(args.cpu_sample, args.cpu_omega)), flush=True)
+        return
     rank, world, local, pg = dist_setup(args.gpus)
     if args.impl == "reference":
         run_reference(args, rank, world, pg)
