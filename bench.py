@@ -43,7 +43,7 @@ UNIT = "ms/solve"
 SEEDS = [(s, "gaussian" if s % 2 == 0 else "binary") for s in range(8)]
 # DRAM bytes (read + write) of one k_sor_cluster_rr launch of the autotuned
 # headline solve, ncu (profiles/k_sor_cluster_rr_512_autotuned.md)
-CLUSTER_DRAM_BYTES_PER_LAUNCH = 2.164992e6
+CLUSTER_DRAM_BYTES_PER_LAUNCH = 2.183e6
 # FP64 operations per cell-sweep of the block schedule's update and the
 # measured FP64 FMA rate of this part (dependent-free FMA loop, all SMs)
 FP64_OPS_PER_CELL = 5
@@ -70,6 +70,10 @@ def parse():
     ap.add_argument("--config4", action="store_true",
                     help="instead of the headline: the full caustic pipeline at a 1024^2 mesh on 4096^2 grids "
                          "(transport and height iterations, plain FP64 and mixed), one JSON line")
+    ap.add_argument("--pipeline-profile", action="store_true",
+                    help="one caustic design at the 1024^2-mesh / 4096^2-grid size: initialisation, one transport "
+                         "and one height iteration with the solves capped at 8 sweeps (for profiling the "
+                         "pipeline kernels), per-step device times as one JSON line")
     ap.add_argument("--cpu-sample", type=float, default=None, metavar="BUDGET_S",
                     help="internal: time the reference's CPU solver on the eight densities in this fresh process "
                          "(per-solve budget BUDGET_S) and print one JSON object")
@@ -603,6 +607,42 @@ def run_ours(args, rank, world, local, pg):
     ctx.close()
 
 
+def run_pipeline_profile(local):
+    """The pipeline kernels at the 1024^2-mesh / 4096^2-grid size (fields of
+    128 MiB, beyond the L2): one design's initialisation, one transport and
+    one height iteration in mixed precision with each Poisson solve capped at 8
+    sweeps, so that a launch list of this run is the pipeline's own kernels."""
+    import torch
+
+    import poisson_caustic_design_gb300 as pcd
+
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    ctx = pcd.Context(local)
+    R, N = 1024, 4096
+    cap = pcd.SolveOptions(tol=1e-7, precision=pcd.PREC_MIXED, omega=-1.0, max_iterations=8)
+    d = pcd.CausticDesign(ctx, transport=cap, height_solve=cap)
+    d.set_mesh_resolution(R, R)
+    d.set_domain_resolution(N, N)
+    d.set_mesh_size(0.5, 0.5)
+    d.set_lens_focal_length(1.5)
+    d.set_lens_thickness(0.1)
+    img = pcd.inputs.pipeline_image(R, seed=4)
+    out = {"mesh": R, "grid": N}
+    for name, fn in (("init", lambda: d.initialize_solvers(img)), ("transport", d.perform_transport_iteration),
+                     ("height", lambda: d.perform_height_map_iteration(0))):
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        fn()
+        torch.cuda.synchronize()
+        out[name + "_ms"] = (time.perf_counter() - t) * 1e3
+        if name != "init":
+            out[name + "_solve_ms"] = d.last_solve_stats["device_ms"]
+    print(json.dumps({"pipeline_profile": out}), flush=True)
+    d.close()
+    ctx.close()
+
+
 def run_config4(args, local):
     """Full pipeline at mesh 1024^2 / grid 4096^2 on one target: target-area
     initialisation, two transport iterations and one height iteration, with the
@@ -684,6 +724,9 @@ def main():
     elif args.config4:
         if rank == 0:
             run_config4(args, local)
+    elif args.pipeline_profile:
+        if rank == 0:
+            run_pipeline_profile(local)
     else:
         run_ours(args, rank, world, local, pg)
     if pg is not None:

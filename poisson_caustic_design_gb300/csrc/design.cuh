@@ -31,6 +31,7 @@ struct Design {
     double *pixels = nullptr, *raster = nullptr, *phi = nullptr, *h = nullptr;
     double *norm_x = nullptr, *norm_y = nullptr, *div = nullptr;
     unsigned int *owner = nullptr;  // point-location owner per query
+    double *qc = nullptr;           // query coordinates: raster sample x, y; shrunk source vertex x, y
     // reductions
     double *scratch = nullptr;
     unsigned int *counter = nullptr;

@@ -28,16 +28,27 @@ __device__ __forceinline__ bool is_last_block(unsigned int *counter)
     return last;
 }
 
+// NaN by its bit pattern (integer instructions: the FP64 pipe of this part
+// runs at 1/56 of the FP32 rate, and a per-cell FP64 compare would make the
+// mean removal FP64-bound instead of HBM-bound).
+__device__ __forceinline__ bool is_nan_bits(double x)
+{
+    return (__double_as_longlong(x) & 0x7fffffffffffffffll) > 0x7ff0000000000000ll;
+}
+
 // Pass 1: per-block NaN-skipping (sum, count); the last block folds them into
-// the mean (scratch[0]) and resets the counter.
+// the mean (scratch[0]) and resets the counter.  Per cell one FP64 addition;
+// the count is an integer until the block reduction.
 __global__ void __launch_bounds__(kT) k_mean(const double *__restrict__ g, long n, double *scratch,
                                              unsigned int *counter)
 {
     double v[2] = {0.0, 0.0};
+    long cnt = 0;
     for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
-        double x = g[i];
-        if (!isnan(x)) { v[0] += x; v[1] += 1.0; }
+        const double x = g[i];
+        if (!is_nan_bits(x)) { v[0] += x; cnt++; }
     }
+    v[1] = (double)cnt;
     block_reduce<2, 0u>(v);
     if (threadIdx.x == 0) {
         scratch[2 + 2 * blockIdx.x] = v[0];
@@ -63,8 +74,8 @@ __global__ void __launch_bounds__(kT) k_sub_mean(double *__restrict__ g, long n,
 {
     const double avg = scratch[0];
     for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
-        double x = g[i];
-        if (!isnan(x)) g[i] = x - avg;
+        const double x = g[i];
+        if (!is_nan_bits(x)) g[i] = x - avg;
     }
 }
 

@@ -68,26 +68,48 @@ __device__ __forceinline__ void tri_vertices(int t, int nx, int v[3])
 
 // Barycentric coordinates exactly as bvh.cpp:162-190 computes them for the
 // triangle passed as (tri[2], tri[1], tri[0]); bc[k] weights vertex k.
-// Returns the acceptance test of bvh.cpp:208-217.
-__device__ __forceinline__ bool bary(double2 A, double2 B, double2 Cc, double px, double py, double bc[3])
+// Returns the acceptance test of bvh.cpp:208-217.  Split into the triangle's
+// part (edge vectors, Gram entries, the reciprocal of the determinant), done
+// once per triangle, and the point's part: the same operations in the same
+// order as one call, so the same bits.
+struct BaryPre {
+    double cx, cy, v0x, v0y, v1x, v1y, d00, d01, d11, inv;
+};
+
+__device__ __forceinline__ BaryPre bary_pre(double2 A, double2 B, double2 Cc)
 {
-    const double v0x = A.x - Cc.x, v0y = A.y - Cc.y;
-    const double v1x = B.x - Cc.x, v1y = B.y - Cc.y;
-    const double v2x = px - Cc.x, v2y = py - Cc.y;
-    const double d00 = __dadd_rn(__dmul_rn(v0x, v0x), __dmul_rn(v0y, v0y));
-    const double d01 = __dadd_rn(__dmul_rn(v0x, v1x), __dmul_rn(v0y, v1y));
-    const double d02 = __dadd_rn(__dmul_rn(v0x, v2x), __dmul_rn(v0y, v2y));
-    const double d11 = __dadd_rn(__dmul_rn(v1x, v1x), __dmul_rn(v1y, v1y));
-    const double d12 = __dadd_rn(__dmul_rn(v1x, v2x), __dmul_rn(v1y, v2y));
-    const double denom = __dsub_rn(__dmul_rn(d00, d11), __dmul_rn(d01, d01));
-    const double inv = 1.0 / denom;
-    const double u = __dmul_rn(__dsub_rn(__dmul_rn(d11, d02), __dmul_rn(d01, d12)), inv);
-    const double v = __dmul_rn(__dsub_rn(__dmul_rn(d00, d12), __dmul_rn(d01, d02)), inv);
+    BaryPre t;
+    t.cx = Cc.x;
+    t.cy = Cc.y;
+    t.v0x = A.x - Cc.x;
+    t.v0y = A.y - Cc.y;
+    t.v1x = B.x - Cc.x;
+    t.v1y = B.y - Cc.y;
+    t.d00 = __dadd_rn(__dmul_rn(t.v0x, t.v0x), __dmul_rn(t.v0y, t.v0y));
+    t.d01 = __dadd_rn(__dmul_rn(t.v0x, t.v1x), __dmul_rn(t.v0y, t.v1y));
+    t.d11 = __dadd_rn(__dmul_rn(t.v1x, t.v1x), __dmul_rn(t.v1y, t.v1y));
+    const double denom = __dsub_rn(__dmul_rn(t.d00, t.d11), __dmul_rn(t.d01, t.d01));
+    t.inv = 1.0 / denom;
+    return t;
+}
+
+__device__ __forceinline__ bool bary_at(const BaryPre &t, double px, double py, double bc[3])
+{
+    const double v2x = px - t.cx, v2y = py - t.cy;
+    const double d02 = __dadd_rn(__dmul_rn(t.v0x, v2x), __dmul_rn(t.v0y, v2y));
+    const double d12 = __dadd_rn(__dmul_rn(t.v1x, v2x), __dmul_rn(t.v1y, v2y));
+    const double u = __dmul_rn(__dsub_rn(__dmul_rn(t.d11, d02), __dmul_rn(t.d01, d12)), t.inv);
+    const double v = __dmul_rn(__dsub_rn(__dmul_rn(t.d00, d12), __dmul_rn(t.d01, d02)), t.inv);
     const double eps = 1e-12;
     bc[0] = u;
     bc[1] = v;
     bc[2] = __dsub_rn(__dsub_rn(1.0, u), v);
     return (u >= -eps && v >= -eps) && (__dadd_rn(u, v) <= 1.0 + eps);
+}
+
+__device__ __forceinline__ bool bary(double2 A, double2 B, double2 Cc, double px, double py, double bc[3])
+{
+    return bary_at(bary_pre(A, B, Cc), px, py, bc);
 }
 
 __device__ __forceinline__ double sample_coord(int i, int n, double extent)
@@ -307,19 +329,38 @@ __global__ void k_scale_areas(double *areas, int n, const double *total, double 
 // ---- point location ---------------------------------------------------------
 // mode 0: grid samples (x_i, y_j) of mesh.cpp:241-254 on an rx x ry grid;
 // mode 1: shrunk source vertices eps + s*((w-2eps)/w) of mesh.cpp:356-360.
+// Both are separable, x from the column and y from the row, so their
+// coordinates (each with an FP64 division) are computed once per design into
+// per-axis tables cx[qx], cy[qy] (k_query_coords) and looked up.
 struct QueryGrid {
     int mode;
     int qx, qy;  // query grid extents
     int nx, ny;  // mesh resolution
     double width, height;
+    const double *cx, *cy;  // the query coordinates of each column and row
 };
 
-__device__ __forceinline__ double2 query_point(const QueryGrid &g, int ix, int iy)
+__device__ __forceinline__ double2 query_point_direct(const QueryGrid &g, int ix, int iy)
 {
     if (g.mode == 0) return make_double2(sample_coord(ix, g.qx, g.width), sample_coord(iy, g.qy, g.height));
     const double2 s = source_xy(iy * g.nx + ix, g.nx, g.ny, g.width, g.height);
     return make_double2(__dadd_rn(kSampleEps, __dmul_rn(s.x, __ddiv_rn(g.width - 2 * kSampleEps, g.width))),
                         __dadd_rn(kSampleEps, __dmul_rn(s.y, __ddiv_rn(g.height - 2 * kSampleEps, g.height))));
+}
+
+__device__ __forceinline__ double2 query_point(const QueryGrid &g, int ix, int iy)
+{
+    return make_double2(__ldg(g.cx + ix), __ldg(g.cy + iy));
+}
+
+// The coordinate tables of a query grid: column ix's x from row 0, row iy's
+// y from column 0 (the formulas above give every point of a column the same x).
+__global__ void k_query_coords(QueryGrid g, double *cx, double *cy)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < g.qx + g.qy; i += gridDim.x * blockDim.x) {
+        if (i < g.qx) cx[i] = query_point_direct(g, i, 0).x;
+        else cy[i - g.qx] = query_point_direct(g, 0, i - g.qx).y;
+    }
 }
 
 __device__ __forceinline__ void query_range(const QueryGrid &g, double lo, double hi, int n, double extent, bool is_x,
@@ -352,14 +393,16 @@ __global__ void k_scatter_owner(const double2 *__restrict__ pts, QueryGrid g, un
         int ilo, ihi, jlo, jhi;
         query_range(g, xmin, xmax, g.qx, g.width, true, ilo, ihi);
         query_range(g, ymin, ymax, g.qy, g.height, false, jlo, jhi);
-        for (int jy = jlo; jy <= jhi; jy++)
+        const BaryPre pre = bary_pre(A, B, Cc);
+        for (int jy = jlo; jy <= jhi; jy++) {
+            const double py = __ldg(g.cy + jy);
             for (int ix = ilo; ix <= ihi; ix++) {
                 const long s = (long)jy * g.qx + ix;
                 if (owner[s] <= (unsigned)t) continue;  // a lower triangle already holds it
-                const double2 p = query_point(g, ix, jy);
                 double bc[3];
-                if (bary(A, B, Cc, p.x, p.y, bc)) atomicMin(&owner[s], (unsigned)t);
+                if (bary_at(pre, __ldg(g.cx + ix), py, bc)) atomicMin(&owner[s], (unsigned)t);
             }
+        }
     }
 }
 
@@ -656,6 +699,19 @@ __global__ void k_count_folds(const double2 *__restrict__ tp, int nx, int ny, un
     if ((threadIdx.x & 31) == 0 && local) atomicAdd(count, local);
 }
 
+// The query grid of a design: mode 0 its rx x ry raster samples, mode 1 its
+// shrunk source vertices, with the coordinate tables filled at initialisation
+// (qc: rx sample x, ry sample y, nx source x, ny source y).
+QueryGrid query_grid(const Design &d, int mode)
+{
+    const pcd_design_params &p = d.p;
+    QueryGrid g{mode, mode ? p.mesh_res_x : p.res_x, mode ? p.mesh_res_y : p.res_y, p.mesh_res_x, p.mesh_res_y,
+                p.width, p.height, nullptr, nullptr};
+    g.cx = mode ? d.qc + p.res_x + p.res_y : d.qc;
+    g.cy = g.cx + g.qx;
+    return g;
+}
+
 }  // namespace
 
 // ---------------------------------------------------------------------------
@@ -673,6 +729,7 @@ int Design::alloc()
     double **gbufs[] = {&pixels, &raster, &phi, &h, &norm_x, &norm_y, &div};
     for (double **b : gbufs) PCD_CUDA(cudaMalloc(b, ng * sizeof(double)));
     PCD_CUDA(cudaMalloc(&owner, nq * sizeof(unsigned int)));
+    PCD_CUDA(cudaMalloc(&qc, sizeof(double) * ((size_t)p.res_x + p.res_y + p.mesh_res_x + p.mesh_res_y)));
     PCD_CUDA(cudaMalloc(&scratch, sizeof(double) * (4 + 2 * 4096)));
     PCD_CUDA(cudaMalloc(&counter, 4 * sizeof(unsigned int)));
     PCD_CUDA(cudaMemset(counter, 0, 4 * sizeof(unsigned int)));
@@ -684,7 +741,7 @@ int Design::alloc()
 void Design::release()
 {
     void *bufs[] = {tp, src_xy, pts_out, inv, sz, target_areas, areas, errors, vgx, vgy, nrm_x, nrm_y, hv, pixels, raster,
-                    phi, h, norm_x, norm_y, div, owner, scratch, counter, small};
+                    phi, h, norm_x, norm_y, div, owner, scratch, counter, small, qc};
     for (void *b : bufs)
         if (b) cudaFree(b);
     if (small_host) cudaFreeHost(small_host);
@@ -692,14 +749,14 @@ void Design::release()
     pts_out = sz = target_areas = areas = errors = vgx = vgy = nrm_x = nrm_y = hv = nullptr;
     pixels = raster = phi = h = norm_x = norm_y = div = nullptr;
     owner = counter = nullptr;
-    scratch = nullptr;
+    scratch = qc = nullptr;
     small = small_host = nullptr;
     initialized = false;
 }
 
 int Design::locate(const double2 *pts, int mode, int qx, int qy, cudaStream_t s)
 {
-    QueryGrid g{mode, qx, qy, p.mesh_res_x, p.mesh_res_y, p.width, p.height};
+    const QueryGrid g = query_grid(*this, mode);
     PCD_CUDA(cudaMemsetAsync(owner, 0xFF, sizeof(unsigned int) * (size_t)qx * qy, s));
     const int ntri = 2 * (p.mesh_res_x - 1) * (p.mesh_res_y - 1);
     k_scatter_owner<<<nblocks(ntri), kT, 0, s>>>(pts, g, owner);
@@ -712,7 +769,7 @@ int Design::raster_values(const double2 *pts, const double *va, const double *vb
 {
     const int rx = p.res_x, ry = p.res_y;
     PCD_TRY(locate(pts, 0, rx, ry, s));
-    QueryGrid g{0, rx, ry, p.mesh_res_x, p.mesh_res_y, p.width, p.height};
+    const QueryGrid g = query_grid(*this, 0);
     unsigned int *miss = (unsigned int *)small;
     PCD_CUDA(cudaMemsetAsync(miss, 0, sizeof(unsigned int), s));
     k_raster_gather<<<nblocks((long)rx * ry, 4096), kT, 0, s>>>(pts, g, owner, va, vb, oa, ob, miss);
@@ -740,6 +797,12 @@ int Design::initialize(const double *image_host)
     k_mesh_init<<<nblocks(nv), kT, 0, s>>>(tp, sz, nx, ny, p.width, p.height);
     PCD_LAUNCHED(1);
     PCD_CUDA(cudaMemcpyAsync(src_xy, tp, nv * sizeof(double2), cudaMemcpyDeviceToDevice, s));
+    // coordinate tables of the two query grids (raster samples, source vertices)
+    for (int mode = 0; mode < 2; mode++) {
+        const QueryGrid g = query_grid(*this, mode);
+        k_query_coords<<<nblocks(g.qx + g.qy), kT, 0, s>>>(g, const_cast<double *>(g.cx), const_cast<double *>(g.cy));
+        PCD_LAUNCHED(1);
+    }
     // target areas (caustic_design.cpp:348)
     const int vb = nblocks(nv, 2048);
     k_target_areas<<<vb, kT, 0, s>>>(tp, pixels, rx, ry, p.width, nx, ny, target_areas, scratch, counter);
@@ -813,7 +876,7 @@ int Design::height_iteration(int itr, double *update_out, pcd_solve_stats *stats
     const int nv = nx * ny;
     // inverse transport map (mesh.cpp:348-409)
     PCD_TRY(locate(tp, 1, nx, ny, s));
-    QueryGrid g{1, nx, ny, nx, ny, p.width, p.height};
+    const QueryGrid g = query_grid(*this, 1);
     unsigned int *miss = (unsigned int *)small;
     PCD_CUDA(cudaMemsetAsync(miss, 0, sizeof(unsigned int), s));
     k_inverse_gather<<<nblocks(nv), kT, 0, s>>>(tp, g, owner, inv, miss);
@@ -932,7 +995,7 @@ int Design::get_vertices(int which, double *out)
             return PCD_BAD_ARG;
         }
         PCD_TRY(locate(tp, 1, nx, ny, s));
-        QueryGrid g{1, nx, ny, nx, ny, p.width, p.height};
+        const QueryGrid g = query_grid(*this, 1);
         unsigned int *miss = (unsigned int *)small;
         PCD_CUDA(cudaMemsetAsync(miss, 0, sizeof(unsigned int), s));
         k_inverse_gather<<<nblocks(nv), kT, 0, s>>>(tp, g, owner, inv, miss);
