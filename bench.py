@@ -59,6 +59,8 @@ def parse():
     ap.add_argument("--cpu-budget-s", type=float, default=20.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
+    ap.add_argument("--no-pipelines", action="store_true",
+                    help="skip the full-pipeline sections (mesh 128 and mesh 1024 designs)")
     ap.add_argument("--headline-only", action="store_true",
                     help="time only the headline form (skips the other forms, the accuracy and end-to-end "
                          "sections, the batch and the 4096^2 sections): for profiling the headline step")
@@ -79,6 +81,9 @@ def parse():
                          "(per-solve budget BUDGET_S) and print one JSON object")
     ap.add_argument("--cpu-omega", choices=["reference", "neumann"], default="reference",
                     help="internal, with --cpu-sample: the reference's omega or the Neumann-optimal one")
+    ap.add_argument("--cpu-what", choices=["solve", "config0", "config4"], default="solve",
+                    help="internal, with --cpu-sample: the single solves, the full-pipeline workload's first "
+                         "transport iteration, or the 4096^2 per-sweep time")
     return ap.parse_args()
 
 
@@ -254,12 +259,50 @@ def cpu_sample(budget_s, omega_kind="reference", seeds=None):
             "per_solve": per}
 
 
-def cpu_sample_subprocess(budget_s, omega_kind="reference"):
-    """cpu_sample in a fresh interpreter: no CUDA context and no runtime
-    threads of this process compete with the solver's fork-join threads."""
+def cpu_pipeline_sample(what):
+    """The reference's pipeline on the host with its threaded solver: config0
+    = initialisation and first transport iteration of the 128^2-mesh design
+    (the C port of caustic_design.cpp:190-266,334-364; the reference's own
+    1e-7 max-update solve on all host threads); config4 = the threaded SOR's
+    time per sweep on a 4096^2 grid."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+
+    from poisson_caustic_design_gb300 import inputs
+
+    oracle.build(ref=False)
+    port = oracle.Port()
+    threads = os.cpu_count() or 1
+    seg = int(np.floor(np.sqrt(threads)))
+    if what == "config4":
+        b = inputs.poisson_rhs(4096, 3, "gaussian")
+        phi = np.zeros_like(b)
+        port.poisson_solver_threads(b, phi, 2, 0.0, threads)
+        t = time.perf_counter()
+        port.poisson_solver_threads(b, phi, 6, 0.0, threads)
+        return {"per_sweep_ms": (time.perf_counter() - t) / 6 * 1e3, "threads": seg * seg}
+
+    class Threaded(oracle.Port):
+        def poisson_solver(self, D, phi, max_iterations=100000, tol=1e-7):
+            return self.poisson_solver_threads(D, phi, max_iterations, tol, threads)
+
+    d = oracle.PortDesign(Threaded(), 128, 128, 512, 512, 0.5, 0.5, 1.5, 0.1)
+    t = time.perf_counter()
+    d.initialize(inputs.pipeline_image(128, 47))
+    t_init = time.perf_counter() - t
+    t = time.perf_counter()
+    step = d.transport_iteration()
+    return {"init_ms": t_init * 1e3, "first_transport_ms": (time.perf_counter() - t) * 1e3, "step": step,
+            "sweeps": d.sweeps, "threads": seg * seg}
+
+
+def cpu_sample_subprocess(budget_s, omega_kind="reference", what="solve"):
+    """cpu_sample (or cpu_pipeline_sample) in a fresh interpreter: no CUDA
+    context and no runtime threads of this process compete with the solver's
+    fork-join threads."""
     env = {**os.environ, "WORLD_SIZE": "1", "RANK": "0"}
     r = subprocess.run([sys.executable, os.path.abspath(__file__), "--cpu-sample", str(budget_s), "--cpu-omega",
-                        omega_kind], capture_output=True, text=True, env=env)
+                        omega_kind, "--cpu-what", what], capture_output=True, text=True, env=env)
     lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
     if r.returncode != 0 or not lines:
         raise RuntimeError(f"CPU baseline subprocess failed ({r.returncode}): {r.stderr[-500:]}")
@@ -344,6 +387,122 @@ def stream_section(ctx, stream, peak):
         ach = bpc * n4 * n4 / per_sweep / 1e9
         out[nm] = {"us_per_sweep": per_sweep * 1e6, "achieved_gbs": ach, "frac_hbm": ach / peak,
                    "schedule": int(st4["schedule_used"])}
+    return out
+
+
+def _design(pcd, ctx, R, N, transport=None, height=None):
+    d = pcd.CausticDesign(ctx, transport=transport, height_solve=height)
+    d.set_mesh_resolution(R, R)
+    d.set_domain_resolution(N, N)
+    d.set_mesh_size(0.5, 0.5)
+    d.set_lens_focal_length(1.5)
+    d.set_lens_thickness(0.1)
+    return d
+
+
+def config0_section(pcd, ctx, batch=16):
+    """The full-pipeline workload: mesh 128^2 on 512^2 grids, width 0.5,
+    focal length 1.5, thickness 0.1, conv 0.01 (the reference's main.cpp
+    sequence: transport iterations until the step falls below conv, then 3
+    height iterations) on the seeded target of the committed reference golden
+    (tests/golden/pipeline_r128.npz, written by the reference's own compiled
+    Caustic_design).  Plain FP64 with the reference's solves (max |delta| <
+    1e-7 / 1e-8, its omega) and mixed precision with the same stops; the plain
+    form's final points and heights against the reference's; then `batch`
+    designs of different targets as one batch of contexts."""
+    import torch
+
+    z = np.load(os.path.join(ROOT, "tests", "golden", "pipeline_r128.npz"))
+    R, conv, seed = int(z["params"][0]), float(z["params"][4]), int(z["params"][5])
+    N = 4 * R
+    out = {"mesh": R, "grid": N, "conv": conv, "forms": {}}
+    for name, prec in (("plain_fp64", pcd.PREC_FP64), ("mixed", pcd.PREC_MIXED)):
+        d = _design(pcd, ctx, R, N, pcd.SolveOptions(tol=1e-7, precision=prec),
+                    pcd.SolveOptions(tol=1e-8, precision=prec))
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        d.initialize_solvers(pcd.inputs.pipeline_image(R, seed))
+        t1 = time.perf_counter()
+        steps, sweeps, first = [], 0, None
+        for _ in range(50):
+            steps.append(d.perform_transport_iteration())
+            sweeps += d.last_solve_stats["sweeps"]
+            if first is None:
+                torch.cuda.synchronize()
+                first = (time.perf_counter() - t1) * 1e3
+            if steps[-1] < conv:
+                break
+        t2 = time.perf_counter()
+        for itr in range(3):
+            d.perform_height_map_iteration(itr)
+        torch.cuda.synchronize()
+        t3 = time.perf_counter()
+        tp, sp = d.target_points(), d.source_points()
+        zr, zt = z["source_points"][:, 2], z["target_points"]
+        rec = {"total_ms": (t3 - t0) * 1e3, "init_ms": (t1 - t0) * 1e3, "transport_ms": (t2 - t1) * 1e3,
+               "height_ms": (t3 - t2) * 1e3, "first_transport_ms": first, "transport_iterations": len(steps),
+               "reference_transport_iterations": len(z["steps"]), "transport_sweeps": sweeps,
+               "target_points_rel_l2_vs_reference": float(np.linalg.norm(tp - zt) / np.linalg.norm(zt)),
+               "target_points_max_abs_vs_reference": float(np.abs(tp - zt).max()),
+               "vertex_heights_rel_l2_vs_reference": float(np.linalg.norm(sp[:, 2] - zr) / np.linalg.norm(zr))}
+        out["forms"][name] = rec
+        d.close()
+    # `batch` targets (seeds 0..batch-1) on contexts of their own, one batch
+    ctxs = [pcd.Context(ctx.device) for _ in range(batch)]
+    ds = [_design(pcd, c, R, N) for c in ctxs]
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    pcd.initialize_batch(ds, [pcd.inputs.pipeline_image(R, s) for s in range(batch)])
+    live = list(ds)
+    iters = 0
+    while live and iters < 50:
+        st = pcd.transport_iteration_batch(live)
+        iters += 1
+        live = [d for d, s in zip(live, st) if not s < conv]
+    for itr in range(3):
+        pcd.height_iteration_batch(ds, itr)
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    out["batched"] = {"targets": batch, "form": "plain_fp64", "wall_ms": (t1 - t0) * 1e3,
+                      "ms_per_target": (t1 - t0) * 1e3 / batch, "rounds_of_transport_iterations": iters,
+                      "single_target_ms": out["forms"]["plain_fp64"]["total_ms"]}
+    for d in ds:
+        d.close()
+    for c in ctxs:
+        c.close()
+    return out
+
+
+def config4_section(pcd, ctx, batch=16):
+    """The largest workload: mesh 1024^2 on 4096^2 grids.  `batch` targets
+    (seeds 0..batch-1) initialised and taken through their first transport
+    iteration (the costliest: phi starts at 0) as one batch of contexts, mixed
+    precision with the reference's stop (max |delta| < 1e-7, Neumann-optimal
+    omega); the conv 0.001 loop would take minutes per target, so this is a
+    bounded sample of it."""
+    import torch
+
+    R, N = 1024, 4096
+    ctxs = [pcd.Context(ctx.device) for _ in range(batch)]
+    tr = pcd.SolveOptions(tol=1e-7, precision=pcd.PREC_MIXED, omega=-1.0, max_iterations=200000)
+    ds = [_design(pcd, c, R, N, tr, tr) for c in ctxs]
+    imgs = [pcd.inputs.pipeline_image(R, s) for s in range(batch)]
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    pcd.initialize_batch(ds, imgs)
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    steps = pcd.transport_iteration_batch(ds)
+    torch.cuda.synchronize()
+    t2 = time.perf_counter()
+    sweeps = [d.last_solve_stats["sweeps"] for d in ds]
+    out = {"mesh": R, "grid": N, "targets": batch, "form": "mixed", "init_ms": (t1 - t0) * 1e3,
+           "first_transport_ms": (t2 - t1) * 1e3, "ms_per_target_transport": (t2 - t1) * 1e3 / batch,
+           "sweeps_mean": float(np.mean(sweeps)), "steps_finite": bool(np.all(np.isfinite(steps)))}
+    for d in ds:
+        d.close()
+    for c in ctxs:
+        c.close()
     return out
 
 
@@ -560,6 +719,24 @@ def run_ours(args, rank, world, local, pg):
     if not args.no_batch and not args.headline_only:
         stream_roof = stream_section(ctx, stream, peak)
 
+    # the full-pipeline workloads (mesh 128 and mesh 1024), with the CPU
+    # reference's matching sample timed in a fresh process
+    config0 = config4 = None
+    if not args.no_pipelines and not args.headline_only:
+        config0 = config0_section(pcd, ctx)
+        config4 = config4_section(pcd, ctx)
+        if rank == 0 and not args.no_cpu_baseline:
+            c0 = cpu_sample_subprocess(0.0, what="config0")
+            config0["cpu_reference_first_transport"] = {
+                **c0, "gpu_plain_fp64_first_transport_ms": config0["forms"]["plain_fp64"]["first_transport_ms"],
+                "note": "initialisation and first transport iteration of the same design on the host cores "
+                        "(the C port of the reference's steps, its threaded solver)"}
+            c4 = cpu_sample_subprocess(0.0, what="config4")
+            config4["cpu_reference"] = {**c4, "first_transport_ms_extrapolated": c4["per_sweep_ms"] *
+                                        config4["sweeps_mean"],
+                                        "note": "per-sweep time of the reference's threaded SOR at 4096^2 times "
+                                                "the GPU's mean sweep count (one transport solve takes minutes)"}
+
     cpu = None
     if rank == 0 and not args.no_cpu_baseline and not args.headline_only:
         # the reference's threaded solver on the same eight densities as the
@@ -593,6 +770,8 @@ def run_ours(args, rank, world, local, pg):
         "speedup_plain_over_headline": (results["plain_fp64"]["ms"] / hm["ms"] if "plain_fp64" in results else None),
         "headline_form": headline,
         "batched": batched,
+        "config0_pipeline": config0,
+        "config4_pipeline_batched": config4,
         "roofline_stream_4096": stream_roof,
         "roofline": roof,
         "cpu_baseline": cpu,
@@ -716,7 +895,9 @@ def run_config4(args, local):
 def main():
     args = parse()
     if args.cpu_sample is not None:
-        print(json.dumps(cpu_sample(args.cpu_sample, args.cpu_omega)), flush=True)
+        out = (cpu_sample(args.cpu_sample, args.cpu_omega) if args.cpu_what == "solve"
+               else cpu_pipeline_sample(args.cpu_what))
+        print(json.dumps(out), flush=True)
         return
     rank, world, local, pg = dist_setup(args.gpus)
     if args.impl == "reference":

@@ -390,6 +390,22 @@ int pcd_design_height_iteration(pcd_design *d, int itr, double *update_out, pcd_
 int pcd_design_get_grid(pcd_design *d, int which, double *host_out);
 int pcd_design_get_vertices(pcd_design *d, int which, double *host_out);
 
+/* Batched designs (no counterpart in the reference, which runs one
+ * Caustic_design per process): the same call on n designs (1..1024) at
+ * once.  Each design runs on a host thread of its own and its work stays on
+ * its context's stream, so designs created on distinct contexts overlap on
+ * the GPU wherever one design leaves SMs idle (a 512^2 mixed-precision solve
+ * occupies one 16-SM cluster); designs sharing a context run one after the
+ * other.  Results are those of the single calls.  steps / updates /
+ * statuses / stats / images have n entries (stats and statuses may be NULL);
+ * the return value is PCD_OK or the first failing design's status, whose
+ * text pcd_last_error() gives on the calling thread. */
+int pcd_design_initialize_batch(pcd_design *const *designs, int n, const double *const *images, int *statuses);
+int pcd_design_transport_iteration_batch(pcd_design *const *designs, int n, double *steps, pcd_solve_stats *stats,
+                                         int *statuses);
+int pcd_design_height_iteration_batch(pcd_design *const *designs, int n, int itr, double *updates,
+                                      pcd_solve_stats *stats, int *statuses);
+
 #ifdef __cplusplus
 }
 #endif

@@ -14,5 +14,5 @@ from .solver import (PREC_FP64, PREC_MIXED, SCHED_AUTO, SCHED_CLUSTER, SCHED_LAU
                      SCHED_PERSISTENT, SCHED_STREAM, SCHED_STRIPES, SCHED_TILES, SCHED_BLOCKS,
                      STOP_MAX_UPDATE, STOP_REL_RESIDUAL, Context, SolveOptions, batch_solve, poisson_solver,
                      solver_progress)
-from .caustic_design import (CausticDesign, export_grid_to_svg, save_heightmap_as_json,  # noqa: F401
-                             save_solid_obj)
+from .caustic_design import (CausticDesign, export_grid_to_svg, height_iteration_batch,  # noqa: F401
+                             initialize_batch, save_heightmap_as_json, save_solid_obj, transport_iteration_batch)

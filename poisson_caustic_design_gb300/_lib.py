@@ -175,6 +175,11 @@ SIGNATURES = {
     "pcd_design_initialize": (C.c_int, [_vp, _vp]),
     "pcd_design_transport_iteration": (C.c_int, [_vp, _dp, C.POINTER(SolveStats)]),
     "pcd_design_height_iteration": (C.c_int, [_vp, C.c_int, _dp, C.POINTER(SolveStats)]),
+    "pcd_design_initialize_batch": (C.c_int, [_vp, C.c_int, _vp, C.POINTER(C.c_int)]),
+    "pcd_design_transport_iteration_batch": (C.c_int, [_vp, C.c_int, _dp, C.POINTER(SolveStats),
+                                                       C.POINTER(C.c_int)]),
+    "pcd_design_height_iteration_batch": (C.c_int, [_vp, C.c_int, C.c_int, _dp, C.POINTER(SolveStats),
+                                                    C.POINTER(C.c_int)]),
     "pcd_design_get_grid": (C.c_int, [_vp, C.c_int, _vp]),
     "pcd_design_get_vertices": (C.c_int, [_vp, C.c_int, _vp]),
 }

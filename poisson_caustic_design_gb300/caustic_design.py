@@ -75,6 +75,12 @@ class CausticDesign:
 
     # ---- iterations ----
     def initialize_solvers(self, image):
+        img = self._create(image)
+        check(self._L.pcd_design_initialize(self._h, img.ctypes.data), "pcd_design_initialize")
+
+    def _create(self, image):
+        """The device design for the current settings (before initialisation);
+        returns the image as a contiguous float64 array."""
         img = np.ascontiguousarray(image, dtype=np.float64)
         if img.shape != (self.resolution_y, self.resolution_x):
             raise ValueError(f"image must be resolution_y x resolution_x = {(self.resolution_y, self.resolution_x)}")
@@ -91,7 +97,7 @@ class CausticDesign:
         h = C.c_void_p()
         check(self._L.pcd_design_create(self._ctx.handle, C.byref(p), C.byref(h)), "pcd_design_create")
         self._h = h
-        check(self._L.pcd_design_initialize(self._h, img.ctypes.data), "pcd_design_initialize")
+        return img
 
     def perform_transport_iteration(self) -> float:
         """Returns the step size; NaN when a raster miss was handled by
@@ -236,3 +242,53 @@ def save_heightmap_as_json(heightmap, filename: str) -> None:
     L = _lib.load()
     check(L.pcd_write_heightmap_json(h.ctypes.data_as(C.POINTER(C.c_double)), h.shape[1], h.shape[0],
                                      filename.encode()), "pcd_write_heightmap_json")
+
+
+# ---- batched designs (no counterpart in the reference) ----------------------
+# The same step on many designs at once: each design runs on a host thread of
+# its own inside the library and its work stays on its context's stream, so
+# designs created on distinct contexts overlap on the GPU.
+
+def _handles(designs):
+    return (C.c_void_p * len(designs))(*[d._h.value for d in designs])
+
+
+def initialize_batch(designs, images):
+    """initialize_solvers on every design at once (images[i] for designs[i])."""
+    imgs = [d._create(im) for d, im in zip(designs, images)]
+    n = len(designs)
+    ptrs = (C.c_void_p * n)(*[im.ctypes.data for im in imgs])
+    L = _lib.load()
+    check(L.pcd_design_initialize_batch(_handles(designs), n, ptrs, (C.c_int * n)()), "pcd_design_initialize_batch")
+
+
+def transport_iteration_batch(designs):
+    """perform_transport_iteration on every design at once; returns the step
+    sizes (each design's solve statistics go to its ``last_solve_stats``)."""
+    n = len(designs)
+    steps = np.zeros(n)
+    st = (_lib.SolveStats * n)()
+    codes = (C.c_int * n)()
+    L = _lib.load()
+    check(L.pcd_design_transport_iteration_batch(_handles(designs), n, steps.ctypes.data_as(_lib._dp), st, codes),
+          "pcd_design_transport_iteration_batch")
+    for d, s, c in zip(designs, st, codes):
+        d.last_solve_stats = s.as_dict()
+        d.last_status = int(c)
+    return steps
+
+
+def height_iteration_batch(designs, itr: int):
+    """perform_height_map_iteration(itr) on every design at once; returns the
+    height updates."""
+    n = len(designs)
+    upd = np.zeros(n)
+    st = (_lib.SolveStats * n)()
+    codes = (C.c_int * n)()
+    L = _lib.load()
+    check(L.pcd_design_height_iteration_batch(_handles(designs), n, int(itr), upd.ctypes.data_as(_lib._dp), st,
+                                              codes), "pcd_design_height_iteration_batch")
+    for d, s, c in zip(designs, st, codes):
+        d.last_solve_stats = s.as_dict()
+        d.last_status = int(c)
+    return upd

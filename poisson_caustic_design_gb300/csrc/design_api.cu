@@ -1,6 +1,9 @@
 // design_api.cu -- C ABI of the Caustic_design replacement (declared in include/pcd.h).
 #include <cstring>
 #include <mutex>
+#include <string>
+#include <thread>
+#include <vector>
 
 #include "api_internal.cuh"
 #include "design.cuh"
@@ -25,6 +28,41 @@ static int live(pcd_design *d)
         return PCD_BAD_ARG;
     }
     return PCD_OK;
+}
+
+// Runs fn(i) for the n designs of a batch, each on a host thread of its own
+// (a design's work stays on its context's stream, so designs of distinct
+// contexts overlap on the GPU).  statuses[i] receives each status; the
+// return value is PCD_OK, or the first failing design's status with its
+// error text moved to the calling thread (errors are per thread).
+// PCD_MESH_SMOOTHED is a result, not a failure, as for the single call.
+template <typename F>
+static int run_batch(pcd_design *const *ds, int n, int *statuses, F fn)
+{
+    if (!ds || n < 1 || n > 1024) {
+        set_error("design batch: 1 to 1024 designs");
+        return PCD_BAD_ARG;
+    }
+    for (int i = 0; i < n; i++) PCD_TRY(live(ds[i]));
+    std::vector<int> st((size_t)n, PCD_OK);
+    std::vector<std::string> err((size_t)n);
+    std::vector<std::thread> th;
+    th.reserve((size_t)n);
+    for (int i = 0; i < n; i++)
+        th.emplace_back([&, i] {
+            st[(size_t)i] = fn(i);
+            if (st[(size_t)i] != PCD_OK) err[(size_t)i] = pcd_last_error();
+        });
+    for (auto &t : th) t.join();
+    int first = PCD_OK;
+    for (int i = 0; i < n; i++) {
+        if (statuses) statuses[i] = st[(size_t)i];
+        if (first == PCD_OK && st[(size_t)i] != PCD_OK && st[(size_t)i] != PCD_MESH_SMOOTHED) {
+            first = st[(size_t)i];
+            set_error("design " + std::to_string(i) + " of the batch: " + err[(size_t)i]);
+        }
+    }
+    return first;
 }
 
 extern "C" {
@@ -104,6 +142,30 @@ int pcd_design_height_iteration(pcd_design *d, int itr, double *update_out, pcd_
     std::lock_guard<std::mutex> lk(d->d.ctx->mu);
     PCD_TRY(ctx_activate(d->d.ctx));
     return d->d.height_iteration(itr, update_out, stats);
+}
+
+int pcd_design_transport_iteration_batch(pcd_design *const *designs, int n, double *steps, pcd_solve_stats *stats,
+                                         int *statuses)
+{
+    if (!steps) return PCD_BAD_ARG;
+    return run_batch(designs, n, statuses, [&](int i) {
+        return pcd_design_transport_iteration(designs[i], steps + i, stats ? stats + i : nullptr);
+    });
+}
+
+int pcd_design_height_iteration_batch(pcd_design *const *designs, int n, int itr, double *updates,
+                                      pcd_solve_stats *stats, int *statuses)
+{
+    if (!updates) return PCD_BAD_ARG;
+    return run_batch(designs, n, statuses, [&](int i) {
+        return pcd_design_height_iteration(designs[i], itr, updates + i, stats ? stats + i : nullptr);
+    });
+}
+
+int pcd_design_initialize_batch(pcd_design *const *designs, int n, const double *const *images, int *statuses)
+{
+    if (!images) return PCD_BAD_ARG;
+    return run_batch(designs, n, statuses, [&](int i) { return pcd_design_initialize(designs[i], images[i]); });
 }
 
 int pcd_design_get_grid(pcd_design *d, int which, double *host_out)

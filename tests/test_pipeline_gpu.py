@@ -335,3 +335,44 @@ def test_full_pipeline_at_workload_size_matches_reference(ctx):
     dz = _rel(sp[:, 2], z["source_points"][:, 2])
     assert dz < 1e-5 + 1.5 * (e_ours + e_ref), (dz, e_ours, e_ref)
     d.close()
+
+
+def test_design_batch_matches_single_designs(ctx):
+    """Batched designs (pcd_design_*_batch): five designs of different target
+    images -- four on contexts of their own, one sharing a context -- run
+    initialisation, four transport iterations and three height iterations as
+    batches; each ends bit-identical to the same design run alone."""
+    import poisson_caustic_design_gb300 as pcd
+
+    r = 32
+
+    def make(c, seed):
+        d = pcd.CausticDesign(c)
+        d.set_mesh_resolution(r, r)
+        d.set_domain_resolution(4 * r, 4 * r)
+        d.set_mesh_size(0.5, 0.5)
+        d.set_lens_focal_length(1.5)
+        d.set_lens_thickness(0.1)
+        return d
+
+    seeds = [11, 12, 13, 14, 15]
+    ctxs = [pcd.Context(0) for _ in range(4)]
+    batch = [make(ctxs[i], s) for i, s in enumerate(seeds[:4])] + [make(ctxs[0], seeds[4])]
+    pcd.initialize_batch(batch, [pcd.inputs.pipeline_image(r, s) for s in seeds])
+    steps = [pcd.transport_iteration_batch(batch) for _ in range(4)]
+    ups = [pcd.height_iteration_batch(batch, itr) for itr in range(3)]
+    for k, s in enumerate(seeds):
+        d = make(ctx, s)
+        d.initialize_solvers(pcd.inputs.pipeline_image(r, s))
+        for it in range(4):
+            assert d.perform_transport_iteration() == steps[it][k]
+        for itr in range(3):
+            assert d.perform_height_map_iteration(itr) == ups[itr][k]
+        assert np.array_equal(d.target_points(), batch[k].target_points())
+        assert np.array_equal(d.source_points(), batch[k].source_points())
+        assert np.array_equal(d.h, batch[k].h)
+        d.close()
+    for d in batch:
+        d.close()
+    for c in ctxs:
+        c.close()
