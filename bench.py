@@ -400,7 +400,7 @@ def _design(pcd, ctx, R, N, transport=None, height=None):
     return d
 
 
-def config0_section(pcd, ctx, batch=16):
+def config0_section(pcd, ctx, device, batch=16):
     """The full-pipeline workload: mesh 128^2 on 512^2 grids, width 0.5,
     focal length 1.5, thickness 0.1, conv 0.01 (the reference's main.cpp
     sequence: transport iterations until the step falls below conv, then 3
@@ -448,7 +448,7 @@ def config0_section(pcd, ctx, batch=16):
         out["forms"][name] = rec
         d.close()
     # `batch` targets (seeds 0..batch-1) on contexts of their own, one batch
-    ctxs = [pcd.Context(ctx.device) for _ in range(batch)]
+    ctxs = [pcd.Context(device) for _ in range(batch)]
     ds = [_design(pcd, c, R, N) for c in ctxs]
     torch.cuda.synchronize()
     t0 = time.perf_counter()
@@ -473,7 +473,7 @@ def config0_section(pcd, ctx, batch=16):
     return out
 
 
-def config4_section(pcd, ctx, batch=16):
+def config4_section(pcd, ctx, device, batch=16):
     """The largest workload: mesh 1024^2 on 4096^2 grids.  `batch` targets
     (seeds 0..batch-1) initialised and taken through their first transport
     iteration (the costliest: phi starts at 0) as one batch of contexts, mixed
@@ -483,7 +483,7 @@ def config4_section(pcd, ctx, batch=16):
     import torch
 
     R, N = 1024, 4096
-    ctxs = [pcd.Context(ctx.device) for _ in range(batch)]
+    ctxs = [pcd.Context(device) for _ in range(batch)]
     tr = pcd.SolveOptions(tol=1e-7, precision=pcd.PREC_MIXED, omega=-1.0, max_iterations=200000)
     ds = [_design(pcd, c, R, N, tr, tr) for c in ctxs]
     imgs = [pcd.inputs.pipeline_image(R, s) for s in range(batch)]
@@ -723,8 +723,8 @@ def run_ours(args, rank, world, local, pg):
     # reference's matching sample timed in a fresh process
     config0 = config4 = None
     if not args.no_pipelines and not args.headline_only:
-        config0 = config0_section(pcd, ctx)
-        config4 = config4_section(pcd, ctx)
+        config0 = config0_section(pcd, ctx, local)
+        config4 = config4_section(pcd, ctx, local)
         if rank == 0 and not args.no_cpu_baseline:
             c0 = cpu_sample_subprocess(0.0, what="config0")
             config0["cpu_reference_first_transport"] = {
