@@ -391,15 +391,22 @@ int pcd_design_get_grid(pcd_design *d, int which, double *host_out);
 int pcd_design_get_vertices(pcd_design *d, int which, double *host_out);
 
 /* Batched designs (no counterpart in the reference, which runs one
- * Caustic_design per process): the same call on n designs (1..1024) at
- * once.  Each design runs on a host thread of its own and its work stays on
- * its context's stream, so designs created on distinct contexts overlap on
- * the GPU wherever one design leaves SMs idle (a 512^2 mixed-precision solve
- * occupies one 16-SM cluster); designs sharing a context run one after the
- * other.  Results are those of the single calls.  steps / updates /
- * statuses / stats / images have n entries (stats and statuses may be NULL);
- * the return value is PCD_OK or the first failing design's status, whose
- * text pcd_last_error() gives on the calling thread. */
+ * Caustic_design per process): the same call on n designs (1..1024, no
+ * design twice) at once.  Two forms:
+ *   lock-step -- every design on one context, and the step's solve options
+ *     (transport / height_solve) the same for all and of the mixed-precision
+ *     relative-residual form: the designs' steps before the solve, then ONE
+ *     batched solve of all their grids (pcd_batch_solve_device: every grid's
+ *     tiles in each launch, so grids too small to fill the GPU alone share
+ *     it), then the steps after the solve.  Each grid reaches the tolerance;
+ *     the iterates differ from single calls' within it.
+ *   concurrent -- otherwise: each design on a host thread of its own, its
+ *     work on its context's stream, so designs on distinct contexts overlap
+ *     on the GPU; results are those of the single calls, bit for bit.
+ * steps / updates / statuses / stats / images have n entries (stats and
+ * statuses may be NULL); the return value is PCD_OK or the first failing
+ * design's status, whose text pcd_last_error() gives on the calling thread
+ * (PCD_MESH_SMOOTHED, as for the single call, is a result). */
 int pcd_design_initialize_batch(pcd_design *const *designs, int n, const double *const *images, int *statuses);
 int pcd_design_transport_iteration_batch(pcd_design *const *designs, int n, double *steps, pcd_solve_stats *stats,
                                          int *statuses);

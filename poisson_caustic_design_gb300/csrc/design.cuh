@@ -43,6 +43,12 @@ struct Design {
     int initialize(const double *image_host);
     int transport_iteration(double *step_out, pcd_solve_stats *stats);
     int height_iteration(int itr, double *update_out, pcd_solve_stats *stats);
+    // The iterations in two halves around their Poisson solve (raster into
+    // phi; div into h), for batches that solve many designs' grids at once.
+    int transport_pre(double *step_out);
+    int transport_post(double *step_out);
+    int height_pre();
+    int height_post(double *update_out);
     int get_grid(int which, double *out);
     int get_vertices(int which, double *out);
     int smooth_target(double f);

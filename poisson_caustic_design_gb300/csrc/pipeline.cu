@@ -818,7 +818,7 @@ int Design::initialize(const double *image_host)
     return PCD_OK;
 }
 
-int Design::transport_iteration(double *step_out, pcd_solve_stats *stats)
+int Design::transport_pre(double *step_out)
 {
     if (!initialized) {
         set_error("pcd_design_transport_iteration: initialize first");
@@ -844,12 +844,16 @@ int Design::transport_iteration(double *step_out, pcd_solve_stats *stats)
         set_error("raster miss: " + std::to_string(misses) + " grid samples outside every triangle");
         return PCD_RASTER_MISS;
     }
-    // subtractAverage + poisson_solver (caustic_design.cpp:221-222)
+    // subtractAverage (caustic_design.cpp:221); the solve of raster into phi follows
     PCD_TRY(subtract_average(ctx->grid, raster, (long)rx * ry, s));
-    pcd_solve_stats st{};
-    int ss = solve_device(ctx->solver, raster, phi, rx, ry, rx, p.transport, &st, s);
-    if (ss != PCD_OK && ss != PCD_NOT_CONVERGED) return ss;
-    if (stats) *stats = st;
+    return PCD_OK;
+}
+
+int Design::transport_post(double *step_out)
+{
+    cudaStream_t s = ctx->stream;
+    const int nx = p.mesh_res_x, ny = p.mesh_res_y, rx = p.res_x, ry = p.res_y;
+    const int nv = nx * ny;
     // gradient, vertex sampling, step_grid, max displacement (caustic_design.cpp:225-265)
     unsigned long long *maxbits = small + 1;
     PCD_CUDA(cudaMemsetAsync(maxbits, 0, sizeof(unsigned long long), s));
@@ -864,9 +868,20 @@ int Design::transport_iteration(double *step_out, pcd_solve_stats *stats)
     return PCD_OK;
 }
 
-int Design::height_iteration(int itr, double *update_out, pcd_solve_stats *stats)
+int Design::transport_iteration(double *step_out, pcd_solve_stats *stats)
 {
-    (void)itr;
+    const int pre = transport_pre(step_out);
+    if (pre != PCD_OK) return pre;
+    // poisson_solver (caustic_design.cpp:222)
+    pcd_solve_stats st{};
+    int ss = solve_device(ctx->solver, raster, phi, p.res_x, p.res_y, p.res_x, p.transport, &st, ctx->stream);
+    if (ss != PCD_OK && ss != PCD_NOT_CONVERGED) return ss;
+    if (stats) *stats = st;
+    return transport_post(step_out);
+}
+
+int Design::height_pre()
+{
     if (!initialized) {
         set_error("pcd_design_height_iteration: initialize first");
         return PCD_BAD_ARG;
@@ -899,13 +914,18 @@ int Design::height_iteration(int itr, double *update_out, pcd_solve_stats *stats
         set_error("raster miss on the source mesh");
         return PCD_RASTER_MISS;
     }
-    // divergence + subtractAverage + solve (caustic_design.cpp:307-311)
+    // divergence + subtractAverage (caustic_design.cpp:307-310); the solve of
+    // div into h follows
     PCD_TRY(divergence(norm_x, norm_y, div, rx, ry, s));
     PCD_TRY(subtract_average(ctx->grid, div, (long)rx * ry, s));
-    pcd_solve_stats st{};
-    int ss = solve_device(ctx->solver, div, h, rx, ry, rx, p.height_solve, &st, s);
-    if (ss != PCD_OK && ss != PCD_NOT_CONVERGED) return ss;
-    if (stats) *stats = st;
+    return PCD_OK;
+}
+
+int Design::height_post(double *update_out)
+{
+    cudaStream_t s = ctx->stream;
+    const int nx = p.mesh_res_x, ny = p.mesh_res_y, rx = p.res_x, ry = p.res_y;
+    const int nv = nx * ny;
     // heights (caustic_design.cpp:323-330)
     const int vb = nblocks(nv, 2048);
     k_height_sample<<<vb, kT, 0, s>>>(h, rx, ry, nx, ny, p.width, p.height, hv, scratch, counter);
@@ -919,6 +939,18 @@ int Design::height_iteration(int itr, double *update_out, pcd_solve_stats *stats
     std::memcpy(&u, small_host + 2, sizeof(double));
     if (update_out) *update_out = u;
     return PCD_OK;
+}
+
+int Design::height_iteration(int itr, double *update_out, pcd_solve_stats *stats)
+{
+    (void)itr;
+    PCD_TRY(height_pre());
+    // poisson_solver on the divergence (caustic_design.cpp:311)
+    pcd_solve_stats st{};
+    int ss = solve_device(ctx->solver, div, h, p.res_x, p.res_y, p.res_x, p.height_solve, &st, ctx->stream);
+    if (ss != PCD_OK && ss != PCD_NOT_CONVERGED) return ss;
+    if (stats) *stats = st;
+    return height_post(update_out);
 }
 
 int Design::smooth_target(double f)

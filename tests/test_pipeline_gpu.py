@@ -376,3 +376,54 @@ def test_design_batch_matches_single_designs(ctx):
         d.close()
     for c in ctxs:
         c.close()
+
+
+def test_design_batch_lockstep_solves_together(ctx):
+    """Lock-step batches: designs on one context whose solves take the
+    mixed-precision relative-residual form share one batched solve per step.
+    Each design's step sizes, target points and heights agree with the same
+    design run alone (whose solves run on the cluster schedule) to within the
+    solve tolerance; every batched solve reaches it."""
+    import poisson_caustic_design_gb300 as pcd
+
+    r = 32
+    tr = pcd.SolveOptions(stop=pcd.STOP_REL_RESIDUAL, tol=1e-10, precision=pcd.PREC_MIXED, omega=-1.0,
+                          max_iterations=200000)
+    hs = pcd.SolveOptions(stop=pcd.STOP_REL_RESIDUAL, tol=1e-11, precision=pcd.PREC_MIXED, omega=-1.0,
+                          max_iterations=200000)
+
+    def make(c, seed):
+        d = pcd.CausticDesign(c, transport=tr, height_solve=hs)
+        d.set_mesh_resolution(r, r)
+        d.set_domain_resolution(4 * r, 4 * r)
+        d.set_mesh_size(0.5, 0.5)
+        d.set_lens_focal_length(1.5)
+        d.set_lens_thickness(0.1)
+        return d
+
+    seeds = [21, 22, 23, 24]
+    shared = pcd.Context(0)
+    batch = [make(shared, s) for s in seeds]
+    pcd.initialize_batch(batch, [pcd.inputs.pipeline_image(r, s) for s in seeds])
+    steps = []
+    for _ in range(4):
+        steps.append(pcd.transport_iteration_batch(batch))
+        for d in batch:
+            st = d.last_solve_stats
+            assert st["converged"] and st["rel_residual"] <= 1e-10 and st["schedule_used"] in (3, 6), st
+    ups = [pcd.height_iteration_batch(batch, itr) for itr in range(3)]
+    for k, s in enumerate(seeds):
+        d = make(ctx, s)
+        d.initialize_solvers(pcd.inputs.pipeline_image(r, s))
+        for it in range(4):
+            np.testing.assert_allclose(d.perform_transport_iteration(), steps[it][k], rtol=1e-7)
+        for itr in range(3):
+            d.perform_height_map_iteration(itr)
+        tp, tb = d.target_points(), batch[k].target_points()
+        assert _rel(tb, tp) < 1e-9
+        sa, sb = d.source_points()[:, 2], batch[k].source_points()[:, 2]
+        assert _rel(sb, sa) < 1e-6
+        d.close()
+    for d in batch:
+        d.close()
+    shared.close()
