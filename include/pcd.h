@@ -350,15 +350,22 @@ int pcd_subtract_average_noalloc(double *g, int width, int height, void *stream)
 /* ---- Caustic_design ----------------------------------------------------- */
 typedef enum {
     PCD_GRID_PHI = 0, PCD_GRID_H = 1, PCD_GRID_RASTER = 2, PCD_GRID_DIVERGENCE = 3,
-    PCD_GRID_NORM_X = 4, PCD_GRID_NORM_Y = 5
+    PCD_GRID_NORM_X = 4, PCD_GRID_NORM_Y = 5,
+    PCD_GRID_PIXELS = 6,       /* the target image scaled to [0, 1] (caustic_design.cpp:335) */
+    PCD_GRID_GRADIENT_X = 7,   /* calculate_gradient(phi) (utils.cpp:3-20, caustic_design.cpp:225), */
+    PCD_GRID_GRADIENT_Y = 8    /* computed from the current phi on request */
 } pcd_grid;
 
 typedef enum {
     PCD_VERT_TARGET_POINTS = 10, PCD_VERT_SOURCE_POINTS = 11, PCD_VERT_TARGET_AREAS = 12,
     PCD_VERT_ERRORS = 13, PCD_VERT_NORMALS_X = 14, PCD_VERT_NORMALS_Y = 15,
     PCD_VERT_GRADIENT_X = 16, PCD_VERT_GRADIENT_Y = 17,
-    PCD_VERT_INVERTED_MAP = 18   /* n x 3: the inverted transport map of the current target mesh
+    PCD_VERT_INVERTED_MAP = 18,  /* n x 3: the inverted transport map of the current target mesh
                                     (mesh.cpp:348-409), computed on request; z = 0 */
+    PCD_VERT_CELL_POINTS = 19    /* n x 3: the target mesh the dual cells of the last transport
+                                    iteration (or of the initialisation) were built from: the
+                                    reference's target_cells (caustic_design.cpp:195-196,343-344)
+                                    are its barycentric dual cells; z = 0 */
 } pcd_vertex_field;
 
 typedef struct {

@@ -29,9 +29,43 @@ from . import _lib
 from ._lib import check
 from .solver import Context, SolveOptions
 
-GRID = {"phi": 0, "h": 1, "raster": 2, "divergence": 3, "norm_x": 4, "norm_y": 5}
+GRID = {"phi": 0, "h": 1, "raster": 2, "divergence": 3, "norm_x": 4, "norm_y": 5, "pixels": 6, "gradient_x": 7,
+        "gradient_y": 8}
 VERT = {"target_points": 10, "source_points": 11, "target_areas": 12, "errors": 13, "normals_x": 14,
-        "normals_y": 15, "vertex_gradient_x": 16, "vertex_gradient_y": 17, "inverted_map": 18}
+        "normals_y": 15, "vertex_gradient_x": 16, "vertex_gradient_y": 17, "inverted_map": 18, "cell_points": 19}
+
+
+def dual_cells(points, nx, ny):
+    """The barycentric dual cell of every vertex of the structured mesh
+    (Mesh::build_target_partitioned_dual_cells, mesh.cpp:174-231): for each
+    triangle around the vertex, the quad (v, mid(v, j), centroid(v, j, k),
+    mid(v, k)) with j, k the triangle's next vertices (edge_centroid and
+    triangle_centroid, mesh.cpp:154-172).  Triangles in the library's fixed
+    order (the reference walks an unordered_set).  Returns one list of 4 x 3
+    quads per vertex."""
+    p = np.asarray(points, dtype=np.float64)
+    cells = []
+    cx = nx - 1
+    for i in range(ny):
+        for j in range(nx):
+            tris = []
+            if i < ny - 1 and j < nx - 1:
+                tris.append((2 * (i * cx + j), 0))
+            if i < ny - 1 and j > 0:
+                tris += [(2 * (i * cx + j - 1), 1), (2 * (i * cx + j - 1) + 1, 1)]
+            if i > 0 and j < nx - 1:
+                tris += [(2 * ((i - 1) * cx + j), 2), (2 * ((i - 1) * cx + j) + 1, 0)]
+            if i > 0 and j > 0:
+                tris.append((2 * ((i - 1) * cx + j - 1) + 1, 2))
+            quads = []
+            for t, pos in tris:
+                c = t >> 1
+                base = (c // cx) * nx + c % cx
+                v = (base, base + 1, base + nx) if t % 2 == 0 else (base + nx, base + 1, base + nx + 1)
+                a, b, d = p[v[pos]], p[v[(pos + 1) % 3]], p[v[(pos + 2) % 3]]
+                quads.append(np.array([a, (a + b) / 2.0, (a + b + d) / 3.0, (a + d) / 2.0]))
+            cells.append(quads)
+    return cells
 
 
 class CausticDesign:
@@ -157,7 +191,7 @@ class CausticDesign:
         check(self._L.pcd_design_get_grid(self._h, GRID[name], out.ctypes.data), "pcd_design_get_grid")
         return out
 
-    _POINT_FIELDS = ("target_points", "source_points", "inverted_map")  # n x 3
+    _POINT_FIELDS = ("target_points", "source_points", "inverted_map", "cell_points")  # n x 3
 
     def _vert(self, name):
         n = self.mesh_res_x * self.mesh_res_y
@@ -181,6 +215,22 @@ class CausticDesign:
     @property
     def normals(self):
         return [self._vert("normals_x"), self._vert("normals_y")]
+
+    pixels = property(lambda self: self._grid("pixels"))
+
+    @property
+    def gradient(self):
+        """calculate_gradient(phi) (caustic_design.cpp:225): [d/dx, d/dy] grids."""
+        return [self._grid("gradient_x"), self._grid("gradient_y")]
+
+    def target_cells(self):
+        """The dual cells of the target mesh that the last transport iteration
+        (or the initialisation) built (caustic_design.cpp:195-196,343-344)."""
+        return dual_cells(self._vert("cell_points"), self.mesh_res_x, self.mesh_res_y)
+
+    # never filled by the reference (caustic_design.cpp reads it only in
+    # commented-out code): an empty list, as there
+    first_target_cells = property(lambda self: [])
 
     def target_points(self):
         return self._vert("target_points")

@@ -21,6 +21,7 @@ struct Design {
     double2 *tp = nullptr;       // target points (x, y)
     double2 *src_xy = nullptr;   // source points (x, y), the undeformed grid
     double2 *inv = nullptr;      // inverted transport map
+    double2 *tp_cells = nullptr; // target points the last dual cells were built from
     double *sz = nullptr;        // source heights
     double *target_areas = nullptr, *areas = nullptr, *errors = nullptr;
     double *vgx = nullptr, *vgy = nullptr;      // vertex gradients
@@ -32,6 +33,7 @@ struct Design {
     double *norm_x = nullptr, *norm_y = nullptr, *div = nullptr;
     unsigned int *owner = nullptr;  // point-location owner per query
     double *qc = nullptr;           // query coordinates: raster sample x, y; shrunk source vertex x, y
+    double *grad = nullptr;         // 2 grids: the gradient of phi, allocated on the first request
     // reductions
     double *scratch = nullptr;
     unsigned int *counter = nullptr;

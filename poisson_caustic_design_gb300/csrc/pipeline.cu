@@ -723,6 +723,7 @@ int Design::alloc()
     PCD_CUDA(cudaMalloc(&tp, nv * sizeof(double2)));
     PCD_CUDA(cudaMalloc(&src_xy, nv * sizeof(double2)));
     PCD_CUDA(cudaMalloc(&inv, nv * sizeof(double2)));
+    PCD_CUDA(cudaMalloc(&tp_cells, nv * sizeof(double2)));
     PCD_CUDA(cudaMalloc(&pts_out, 3 * nv * sizeof(double)));
     double **vbufs[] = {&sz, &target_areas, &areas, &errors, &vgx, &vgy, &nrm_x, &nrm_y, &hv};
     for (double **b : vbufs) PCD_CUDA(cudaMalloc(b, nv * sizeof(double)));
@@ -740,12 +741,13 @@ int Design::alloc()
 
 void Design::release()
 {
-    void *bufs[] = {tp, src_xy, pts_out, inv, sz, target_areas, areas, errors, vgx, vgy, nrm_x, nrm_y, hv, pixels, raster,
+    void *bufs[] = {tp, src_xy, pts_out, inv, tp_cells, grad, sz, target_areas, areas, errors, vgx, vgy, nrm_x, nrm_y, hv, pixels, raster,
                     phi, h, norm_x, norm_y, div, owner, scratch, counter, small, qc};
     for (void *b : bufs)
         if (b) cudaFree(b);
     if (small_host) cudaFreeHost(small_host);
-    tp = src_xy = inv = nullptr;
+    tp = src_xy = inv = tp_cells = nullptr;
+    grad = nullptr;
     pts_out = sz = target_areas = areas = errors = vgx = vgy = nrm_x = nrm_y = hv = nullptr;
     pixels = raster = phi = h = norm_x = norm_y = div = nullptr;
     owner = counter = nullptr;
@@ -797,6 +799,7 @@ int Design::initialize(const double *image_host)
     k_mesh_init<<<nblocks(nv), kT, 0, s>>>(tp, sz, nx, ny, p.width, p.height);
     PCD_LAUNCHED(1);
     PCD_CUDA(cudaMemcpyAsync(src_xy, tp, nv * sizeof(double2), cudaMemcpyDeviceToDevice, s));
+    PCD_CUDA(cudaMemcpyAsync(tp_cells, tp, nv * sizeof(double2), cudaMemcpyDeviceToDevice, s));
     // coordinate tables of the two query grids (raster samples, source vertices)
     for (int mode = 0; mode < 2; mode++) {
         const QueryGrid g = query_grid(*this, mode);
@@ -827,6 +830,8 @@ int Design::transport_pre(double *step_out)
     cudaStream_t s = ctx->stream;
     const int nx = p.mesh_res_x, ny = p.mesh_res_y, rx = p.res_x, ry = p.res_y;
     const int nv = nx * ny;
+    // the mesh the dual cells are built from (target_cells, caustic_design.cpp:195-196)
+    PCD_CUDA(cudaMemcpyAsync(tp_cells, tp, nv * sizeof(double2), cudaMemcpyDeviceToDevice, s));
     // dual-cell areas and errors (caustic_design.cpp:195-209)
     k_areas_errors<<<nblocks(nv), kT, 0, s>>>(tp, target_areas, areas, errors, nx, ny);
     PCD_LAUNCHED(1);
@@ -999,6 +1004,16 @@ int Design::get_grid(int which, double *out)
     case PCD_GRID_DIVERGENCE: src = div; break;
     case PCD_GRID_NORM_X: src = norm_x; break;
     case PCD_GRID_NORM_Y: src = norm_y; break;
+    case PCD_GRID_PIXELS: src = pixels; break;
+    case PCD_GRID_GRADIENT_X:
+    case PCD_GRID_GRADIENT_Y: {
+        // calculate_gradient(phi) (caustic_design.cpp:225), on request
+        const size_t ng = (size_t)p.res_x * p.res_y;
+        if (!grad) PCD_CUDA(cudaMalloc(&grad, 2 * ng * sizeof(double)));
+        PCD_TRY(gradient(phi, grad, grad + ng, p.res_x, p.res_y, ctx->stream));
+        src = which == PCD_GRID_GRADIENT_X ? grad : grad + ng;
+        break;
+    }
     default: set_error("pcd_design_get_grid: unknown grid"); return PCD_BAD_ARG;
     }
     cudaStream_t s = ctx->stream;
@@ -1015,8 +1030,9 @@ int Design::get_vertices(int which, double *out)
     switch (which) {
     case PCD_VERT_TARGET_POINTS:
     case PCD_VERT_SOURCE_POINTS:
-        k_points_out<<<nblocks(nv), kT, 0, s>>>(tp, sz, nx, ny, p.width, p.height,
-                                                 which == PCD_VERT_SOURCE_POINTS, pts_out);
+    case PCD_VERT_CELL_POINTS:
+        k_points_out<<<nblocks(nv), kT, 0, s>>>(which == PCD_VERT_CELL_POINTS ? tp_cells : tp, sz, nx, ny, p.width,
+                                                 p.height, which == PCD_VERT_SOURCE_POINTS, pts_out);
         PCD_LAUNCHED(1);
         PCD_CUDA(cudaMemcpyAsync(out, pts_out, sizeof(double) * 3 * nv, cudaMemcpyDeviceToHost, s));
         PCD_CUDA(cudaStreamSynchronize(s));

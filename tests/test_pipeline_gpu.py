@@ -427,3 +427,32 @@ def test_design_batch_lockstep_solves_together(ctx):
     for d in batch:
         d.close()
     shared.close()
+
+
+def test_design_members_pixels_gradient_and_cells(ctx, port):
+    """The members the reference's Caustic_design keeps beside phi and h
+    (caustic_design.h:16-30): pixels = the image scaled to [0, 1]
+    (caustic_design.cpp:335), gradient = calculate_gradient(phi) (the port's,
+    bit for bit), and target_cells = the barycentric dual cells the last
+    transport iteration was built from, whose shoelace areas are the areas
+    behind that iteration's errors (target / (1 + error))."""
+    z = load_golden("pipeline_r16.npz")
+    d, _ = _design(ctx, z)
+    assert np.array_equal(d.pixels, port.scale_proportional(z["image"], 0.0, 1.0))
+    for _ in range(2):
+        d.perform_transport_iteration()
+    gx, gy = port.gradient(d.phi)
+    g = d.gradient
+    assert np.array_equal(g[0], gx) and np.array_equal(g[1], gy)
+    cells = d.target_cells()
+    assert len(cells) == 16 * 16 and all(2 <= len(c) <= 6 for c in cells)
+
+    def shoelace(q):
+        x, y = q[:, 0], q[:, 1]
+        return 0.5 * np.sum(x * np.roll(y, -1) - np.roll(x, -1) * y)
+
+    areas = np.array([sum(shoelace(q) for q in c) for c in cells])
+    expect = d.target_areas / (1.0 + d.errors)
+    np.testing.assert_allclose(areas, expect, rtol=1e-12)
+    assert d.first_target_cells == []
+    d.close()
