@@ -445,7 +445,7 @@ def test_design_members_pixels_gradient_and_cells(ctx, port):
     g = d.gradient
     assert np.array_equal(g[0], gx) and np.array_equal(g[1], gy)
     cells = d.target_cells()
-    assert len(cells) == 16 * 16 and all(2 <= len(c) <= 6 for c in cells)
+    assert len(cells) == 16 * 16 and all(1 <= len(c) <= 6 for c in cells)
 
     def shoelace(q):
         x, y = q[:, 0], q[:, 1]
