@@ -320,6 +320,13 @@ int pcd_unet_get_grads(pcd_unet *net, float *host);
  * lda/ldb multiples of 8; ksplit > 1 needs ksplit*M*N floats of partials. */
 int pcd_gemm_bf16(const void *A, int lda, const void *B, int ldb, float *C, int ldc, int M, int N, int K,
                   int ksplit, float *partials, void *stream);
+/* The same GEMM on a chosen path: 0 automatic, 1 mma.sync (warp-level
+ * tensor-core fragments through ldmatrix), 2 tcgen05 (TMA loads with the
+ * 128-byte swizzle, tcgen05.mma into a tensor-memory accumulator; A and B
+ * 16-byte aligned).  Path 2 synchronises `stream` and returns PCD_TIMEOUT if
+ * a bounded wait of the kernel gave up.  No counterpart in the reference. */
+int pcd_gemm_bf16_path(const void *A, int lda, const void *B, int ldb, float *C, int ldc, int M, int N, int K,
+                       int ksplit, float *partials, int path, void *stream);
 /* network used by warm_start = PCD_WARM_LEARNED (not owned; NULL clears) */
 int pcd_ctx_set_warm_start_net(pcd_ctx *ctx, pcd_unet *net);
 

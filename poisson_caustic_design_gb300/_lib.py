@@ -169,6 +169,8 @@ SIGNATURES = {
     "pcd_ctx_set_warm_start_net": (C.c_int, [_vp, _vp]),
     "pcd_gemm_bf16": (C.c_int, [_vp, C.c_int, _vp, C.c_int, _vp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _vp,
                                 _vp]),
+    "pcd_gemm_bf16_path": (C.c_int, [_vp, C.c_int, _vp, C.c_int, _vp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
+                                     _vp, C.c_int, _vp]),
     "pcd_design_params_default": (C.c_int, [C.POINTER(DesignParams)]),
     "pcd_design_create": (C.c_int, [_vp, C.POINTER(DesignParams), C.POINTER(_vp)]),
     "pcd_design_destroy": (C.c_int, [_vp]),

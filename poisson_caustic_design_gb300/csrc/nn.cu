@@ -24,6 +24,8 @@ namespace nn {
 namespace {
 
 constexpr int GBM = 128, GBK = 32, GST = 3, GTHREADS = 256;
+// automatic path: the tcgen05 form for GEMMs it takes (nn_tc.cu)
+constexpr bool kTcAuto = false;
 constexpr int SROW = GBK + 8;  // padded shared row: 40 bf16 = 80 bytes
 
 __device__ __forceinline__ unsigned smem_u32(const void *p)
@@ -511,10 +513,17 @@ int gemm(const GemmArgs &g0, cudaStream_t s, float *partials)
         g.Cb = nullptr;
         g.ldc = g.N;
     }
+    const bool tc = g.path == 2 || (g.path == 0 && kTcAuto && gemm_tc_applies(g));
     const int BN = g.N <= 32 ? 32 : (g.N <= 64 ? 64 : 128);
     const dim3 grid((g.N + BN - 1) / BN, (g.M + GBM - 1) / GBM, g.ksplit);
     const size_t smem = gemm_smem(BN);
-    if (BN == 32) {
+    if (tc) {
+        if (((uintptr_t)g.A % 16) || ((uintptr_t)g.B % 16)) {
+            set_error("nn gemm: the tcgen05 path needs 16-byte aligned operands");
+            return PCD_BAD_ARG;
+        }
+        PCD_TRY(gemm_tc(g, s));
+    } else if (BN == 32) {
         PCD_CUDA(cudaFuncSetAttribute(k_gemm<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         k_gemm<32><<<grid, GTHREADS, smem, s>>>(g);
     } else if (BN == 64) {
@@ -524,7 +533,7 @@ int gemm(const GemmArgs &g0, cudaStream_t s, float *partials)
         PCD_CUDA(cudaFuncSetAttribute(k_gemm<128>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         k_gemm<128><<<grid, GTHREADS, smem, s>>>(g);
     }
-    PCD_LAUNCHED(1);
+    if (!tc) PCD_LAUNCHED(1);
     if (g.ksplit > 1) {
         k_splitk_reduce<<<grid1d((long)g.M * g.N), 256, 0, s>>>(partials, g.ksplit, g.M, g.N, g.N, g.bias, g.relu,
                                                                outB, outF, ldo);

@@ -20,6 +20,7 @@ struct GemmArgs {
     __nv_bfloat16 *Cb;       // BF16 output (row stride ldc), or
     float *Cf;               // FP32 output
     int ldc;
+    int path = 0;            // 0 automatic, 1 mma.sync, 2 tcgen05 (TMA + tensor memory)
 };
 
 struct AdamParams {
@@ -29,6 +30,12 @@ struct AdamParams {
 size_t gemm_smem(int BN);
 // partials: ksplit * M * N floats when ksplit > 1
 int gemm(const GemmArgs &g, cudaStream_t s, float *partials);
+// The tcgen05 form (nn_tc.cu): whether it takes g (16-byte aligned operands,
+// M of several 128-row tiles, K >= 64), the launch (split-K partials to
+// g.Cf), and the error word its bounded waits set (PCD_TIMEOUT).
+bool gemm_tc_applies(const GemmArgs &g);
+int gemm_tc(const GemmArgs &g, cudaStream_t s);
+int gemm_tc_error(int *out, bool reset);
 int im2col(const __nv_bfloat16 *in, int B, int H, int W, int C, int ldcin, __nv_bfloat16 *out, int Kp, cudaStream_t s);
 int transpose(const __nv_bfloat16 *in, int rows, int cols, int ldin, __nv_bfloat16 *out, int ldout, cudaStream_t s);
 int flip(const __nv_bfloat16 *Wt, int Cout, int Cin, int Kp, __nv_bfloat16 *Wf, int Kpf, cudaStream_t s);

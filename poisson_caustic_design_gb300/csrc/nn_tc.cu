@@ -1,0 +1,365 @@
+// nn_tc.cu -- the U-Net's BF16 GEMM on the 5th-generation tensor cores
+// (tcgen05, sm_103a).
+//
+// C[M x N] = A[M x K] * B[N x K]^T with A and B BF16 row-major, K contiguous
+// ("TN", the layout of nn::gemm), FP32 accumulation in tensor memory.  One CTA
+// computes a 128 x BN tile of C over its share of K:
+//
+//   * TMA (cp.async.bulk.tensor.2d) loads 128 x 64 tiles of A and BN x 64
+//     tiles of B into shared memory with the 128-byte swizzle, through a ring
+//     of kStages stages (full / empty mbarriers; the transfer size is the
+//     whole box, zero-filled where the box leaves the matrix);
+//   * one thread issues tcgen05.mma.cta_group::1.kind::f16 (M = 128, N = BN,
+//     K = 16 per instruction, both operands K-major, described by shared
+//     memory descriptors whose start address steps 32 bytes per K slice
+//     inside the 128-byte swizzle atom) into a 128-lane x BN-column FP32
+//     accumulator in tensor memory, and tcgen05.commit signals the stage free
+//     once the MMAs that read it are done;
+//   * after the last MMA, warps 0-3 read their 32 lanes (rows) of the
+//     accumulator with tcgen05.ld.32x32b and apply the epilogue of nn::gemm
+//     (bias, ReLU, BF16 or FP32 store, or FP32 split-K partials).
+//
+// The same thread produces and consumes the ring: it refills the stage the
+// previous K tile used once that tile's MMAs have completed, while the MMAs
+// of the current tile run.  Every mbarrier wait is bounded: a wait that runs
+// out records PCD_TIMEOUT in *err, the CTA stops issuing, waits (bounded) for
+// what it has in flight and frees its tensor memory.
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cudaTypedefs.h>
+
+#include <mutex>
+
+#include "nn.cuh"
+
+namespace pcd {
+namespace nn {
+
+namespace {
+
+constexpr int kTcBM = 128, kTcBK = 64, kTcStages = 4, kTcThreads = 128;
+constexpr long long kTcSpin = 1ll << 24;
+
+__device__ __forceinline__ unsigned tc_smem(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(unsigned bar, unsigned count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(unsigned bar, unsigned bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+
+// Bounded wait for phase `parity` of the barrier: true once it completed,
+// false when the poll budget ran out.
+__device__ __forceinline__ bool mbar_wait(unsigned bar, unsigned parity)
+{
+    for (long long it = 0; it < kTcSpin; it++) {
+        unsigned done;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(done)
+            : "r"(bar), "r"(parity)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+__device__ __forceinline__ void tma_load_2d(unsigned dst, const CUtensorMap *map, unsigned bar, int x, int y)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4}], [%2];"
+        ::"r"(dst), "l"(map), "r"(bar), "r"(x), "r"(y)
+        : "memory");
+}
+
+// Shared memory descriptor of a K-major operand tile with the 128-byte
+// swizzle: rows of 128 bytes (64 BF16 of K), 8-row swizzle atoms 1024 bytes
+// apart (stride byte offset), leading byte offset unused for this layout
+// (encoded 1), descriptor version 1 (bits 46-47), swizzle mode 2 (bits 61-63).
+__device__ __forceinline__ unsigned long long smem_desc_sw128(unsigned addr)
+{
+    return (unsigned long long)((addr & 0x3FFFFu) >> 4) | (1ull << 16) | ((unsigned long long)(1024 >> 4) << 32) |
+           (1ull << 46) | (2ull << 61);
+}
+
+// Instruction descriptor of kind::f16: D FP32 (bits 4-5 = 1), A and B BF16
+// (bits 7-9 = 1, 10-12 = 1), both K-major (bits 15, 16 = 0), N >> 3 in bits
+// 17-22, M >> 4 in bits 24-28.
+__host__ __device__ constexpr unsigned idesc_bf16_f32(int M, int N)
+{
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((unsigned)(N >> 3) << 17) | ((unsigned)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma_bf16_tc(unsigned tmem_d, unsigned long long a, unsigned long long b, unsigned idesc,
+                                            unsigned accumulate)
+{
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}"
+        ::"r"(tmem_d), "l"(a), "l"(b), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+
+__device__ __forceinline__ void mma_commit(unsigned bar)
+{
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
+}
+
+template <int BN>
+__global__ void __launch_bounds__(kTcThreads, 1)
+    k_gemm_tc(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB, GemmArgs g, int *err)
+{
+    static_assert(BN == 32 || BN == 64 || BN == 128 || BN == 256, "N tile");
+    constexpr unsigned kStageA = kTcBM * kTcBK * 2, kStageB = BN * kTcBK * 2, kStage = kStageA + kStageB;
+    constexpr int kCols = BN < 32 ? 32 : BN;  // tensor memory columns (a power of 2, >= 32)
+    extern __shared__ __align__(1024) unsigned char tc_buf[];
+    __shared__ __align__(8) unsigned long long bars[2 * kTcStages + 1];
+    __shared__ unsigned tmem_base;
+    __shared__ int s_fail;
+    __shared__ int s_fills[kTcStages];  // loads issued per stage (thread 0)
+
+    // the ring must start on a 1024-byte boundary (the swizzle atom)
+    const unsigned raw = tc_smem(tc_buf);
+    const unsigned ring = (raw + 1023u) & ~1023u;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int bm = blockIdx.y * kTcBM, bn = blockIdx.x * BN;
+    const int KT = (g.K + kTcBK - 1) / kTcBK;
+    const int per = (KT + g.ksplit - 1) / g.ksplit;
+    const int kt0 = blockIdx.z * per, kt1 = min(KT, kt0 + per);
+    const int nk = max(0, kt1 - kt0);
+    const unsigned full0 = tc_smem(&bars[0]), empty0 = tc_smem(&bars[kTcStages]), done = tc_smem(&bars[2 * kTcStages]);
+
+    if (threadIdx.x == 0) {
+        s_fail = 0;
+        for (int s = 0; s < kTcStages; s++) {
+            s_fills[s] = 0;
+            mbar_init(full0 + 8 * s, 1);
+            mbar_init(empty0 + 8 * s, 1);
+        }
+        mbar_init(done, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("prefetch.tensormap [%0];" ::"l"(&mapA) : "memory");
+        asm volatile("prefetch.tensormap [%0];" ::"l"(&mapB) : "memory");
+    }
+    if (warp == 0) {
+        // one warp allocates the accumulator's columns (and frees them at the end)
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(tc_smem(&tmem_base)),
+                     "r"(kCols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const unsigned tmem = tmem_base;
+
+    // ---- producer + MMA issuer: thread 0
+    if (threadIdx.x == 0 && nk > 0) {
+        constexpr unsigned idesc = idesc_bf16_f32(kTcBM, BN);
+        bool ok = true;
+        const int pre = min(nk, kTcStages);
+        for (int i = 0; i < pre; i++) {
+            const unsigned st = ring + (unsigned)i * kStage;
+            mbar_expect_tx(full0 + 8 * i, kStage);
+            tma_load_2d(st, &mapA, full0 + 8 * i, (kt0 + i) * kTcBK, bm);
+            tma_load_2d(st + kStageA, &mapB, full0 + 8 * i, (kt0 + i) * kTcBK, bn);
+            s_fills[i]++;
+        }
+        int issued = pre;
+        for (int i = 0; i < nk && ok; i++) {
+            const int s = i % kTcStages;
+            const unsigned phase = (unsigned)((i / kTcStages) & 1);
+            if (!mbar_wait(full0 + 8 * s, phase)) { ok = false; break; }
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const unsigned a = ring + (unsigned)s * kStage, b = a + kStageA;
+#pragma unroll
+            for (int kk = 0; kk < kTcBK / 16; kk++)
+                mma_bf16_tc(tmem, smem_desc_sw128(a + 32u * kk), smem_desc_sw128(b + 32u * kk), idesc,
+                            (i > 0 || kk > 0) ? 1u : 0u);
+            mma_commit(empty0 + 8 * s);
+            // refill the stage of the previous K tile once its MMAs are done
+            if (i > 0 && issued < nk) {
+                const int ps = (i - 1) % kTcStages;
+                const unsigned pphase = (unsigned)(((i - 1) / kTcStages) & 1);
+                if (!mbar_wait(empty0 + 8 * ps, pphase)) { ok = false; break; }
+                const unsigned st = ring + (unsigned)ps * kStage;
+                mbar_expect_tx(full0 + 8 * ps, kStage);
+                tma_load_2d(st, &mapA, full0 + 8 * ps, (kt0 + issued) * kTcBK, bm);
+                tma_load_2d(st + kStageA, &mapB, full0 + 8 * ps, (kt0 + issued) * kTcBK, bn);
+                s_fills[ps]++;
+                issued++;
+            }
+        }
+        if (ok) {
+            mma_commit(done);  // arrives when every MMA issued above has completed
+        } else {
+            atomicCAS(err, 0, PCD_TIMEOUT);
+            s_fail = 1;
+        }
+    }
+    __syncthreads();
+
+    // ---- epilogue: warps 0-3, thread t <-> accumulator lane / tile row t
+    const bool fail = s_fail != 0 || nk == 0;
+    if (!fail) {
+        if (!mbar_wait(done, 0u)) {
+            atomicCAS(err, 0, PCD_TIMEOUT);
+        } else {
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const int row = bm + warp * 32 + lane;
+#pragma unroll
+            for (int c0 = 0; c0 < BN; c0 += 16) {
+                unsigned r[16];
+                const unsigned addr = tmem + ((unsigned)(warp * 32) << 16) + (unsigned)c0;
+                asm volatile(
+                    "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
+                    "[%16];"
+                    : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+                      "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
+                      "=r"(r[15])
+                    : "r"(addr));
+                asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+                if (row < g.M) {
+#pragma unroll
+                    for (int j = 0; j < 16; j++) {
+                        const int n = bn + c0 + j;
+                        if (n >= g.N) continue;
+                        float v = __uint_as_float(r[j]);
+                        if (g.ksplit > 1) {
+                            g.Cf[((size_t)blockIdx.z * g.M + row) * g.ldc + n] = v;
+                            continue;
+                        }
+                        if (g.bias) v += g.bias[n];
+                        if (g.relu) v = fmaxf(v, 0.f);
+                        if (g.Cb) g.Cb[(size_t)row * g.ldc + n] = __float2bfloat16(v);
+                        else g.Cf[(size_t)row * g.ldc + n] = v;
+                    }
+                }
+            }
+        }
+    } else if (nk == 0 && g.ksplit > 1) {
+        // an empty K share still writes zero partials
+        const int row = bm + warp * 32 + lane;
+        if (row < g.M)
+            for (int n = bn; n < min(g.N, bn + BN); n++) g.Cf[((size_t)blockIdx.z * g.M + row) * g.ldc + n] = 0.f;
+    }
+    if (s_fail != 0 && threadIdx.x == 0) {
+        // let what is still in flight land before the shared memory and the
+        // tensor memory go away: every MMA issued (one more commit), and each
+        // stage's latest load (bounded waits)
+        mma_commit(done);
+        (void)mbar_wait(done, 0u);
+        for (int s = 0; s < kTcStages; s++)
+            if (s_fills[s] > 0) (void)mbar_wait(full0 + 8 * s, (unsigned)((s_fills[s] - 1) & 1));
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0) {
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kCols) : "memory");
+    }
+}
+
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no link
+// against the driver library).
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn()
+{
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    });
+    return fn;
+}
+
+// A 2-D tensor map of a rows x cols BF16 matrix (row stride ld elements) with
+// box rows x 64 columns and the 128-byte swizzle.
+int make_map(CUtensorMap *map, const void *base, int rows, int cols, int ld, int box_rows)
+{
+    auto fn = encode_fn();
+    if (!fn) {
+        set_error("tcgen05 gemm: cuTensorMapEncodeTiled is not available");
+        return PCD_DEVICE_ERROR;
+    }
+    const cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
+    const cuuint64_t strides[1] = {(cuuint64_t)ld * 2};
+    const cuuint32_t box[2] = {(cuuint32_t)kTcBK, (cuuint32_t)box_rows};
+    const cuuint32_t estr[2] = {1, 1};
+    const CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void *>(base), dims, strides, box, estr,
+                          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) {
+        set_error("tcgen05 gemm: cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")");
+        return PCD_DEVICE_ERROR;
+    }
+    return PCD_OK;
+}
+
+int *err_word()
+{
+    static int *w = nullptr;
+    static std::mutex mu;
+    std::lock_guard<std::mutex> lk(mu);
+    if (!w && cudaMalloc(&w, sizeof(int)) == cudaSuccess) cudaMemset(w, 0, sizeof(int));
+    return w;
+}
+
+template <int BN>
+int launch_tc(const CUtensorMap &ma, const CUtensorMap &mb, const GemmArgs &g, cudaStream_t s, int *err)
+{
+    const size_t smem = (size_t)kTcStages * (kTcBM * kTcBK * 2 + BN * kTcBK * 2) + 1024;
+    PCD_CUDA(cudaFuncSetAttribute(k_gemm_tc<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const dim3 grid((g.N + BN - 1) / BN, (g.M + kTcBM - 1) / kTcBM, g.ksplit);
+    k_gemm_tc<BN><<<grid, kTcThreads, smem, s>>>(ma, mb, g, err);
+    PCD_LAUNCHED(1);
+    return PCD_OK;
+}
+
+}  // namespace
+
+bool gemm_tc_applies(const GemmArgs &g)
+{
+    // TMA: 16-byte aligned bases and row strides (ld multiples of 8, checked
+    // by gemm); the tensor-core tile only pays for itself on large M
+    return ((uintptr_t)g.A % 16) == 0 && ((uintptr_t)g.B % 16) == 0 && g.M >= 4 * kTcBM && g.K >= kTcBK;
+}
+
+int gemm_tc(const GemmArgs &g, cudaStream_t s)
+{
+    CUtensorMap ma, mb;
+    const int BN = g.N <= 32 ? 32 : (g.N <= 64 ? 64 : 128);
+    PCD_TRY(make_map(&ma, g.A, g.M, g.K, g.lda, kTcBM));
+    PCD_TRY(make_map(&mb, g.B, g.N, g.K, g.ldb, BN));
+    int *err = err_word();
+    if (!err) {
+        set_error("tcgen05 gemm: no error word");
+        return PCD_DEVICE_ERROR;
+    }
+    if (BN == 32) return launch_tc<32>(ma, mb, g, s, err);
+    if (BN == 64) return launch_tc<64>(ma, mb, g, s, err);
+    return launch_tc<128>(ma, mb, g, s, err);
+}
+
+int gemm_tc_error(int *out, bool reset)
+{
+    int *w = err_word();
+    if (!w) return PCD_DEVICE_ERROR;
+    PCD_CUDA(cudaMemcpy(out, w, sizeof(int), cudaMemcpyDeviceToHost));
+    if (reset) PCD_CUDA(cudaMemset(w, 0, sizeof(int)));
+    return PCD_OK;
+}
+
+}  // namespace nn
+}  // namespace pcd

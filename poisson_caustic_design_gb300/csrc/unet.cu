@@ -672,6 +672,39 @@ int pcd_gemm_bf16(const void *A, int lda, const void *B, int ldb, float *C, int 
     return nn::gemm(g, (cudaStream_t)stream, partials);
 }
 
+int pcd_gemm_bf16_path(const void *A, int lda, const void *B, int ldb, float *C, int ldc, int M, int N, int K,
+                       int ksplit, float *partials, int path, void *stream)
+{
+    if (path < 0 || path > 2) {
+        set_error("pcd_gemm_bf16_path: path must be 0, 1 or 2");
+        return PCD_BAD_ARG;
+    }
+    nn::GemmArgs g{};
+    g.A = (const __nv_bfloat16 *)A;
+    g.lda = lda;
+    g.B = (const __nv_bfloat16 *)B;
+    g.ldb = ldb;
+    g.M = M;
+    g.N = N;
+    g.K = K;
+    g.ksplit = ksplit;
+    g.Cf = C;
+    g.ldc = ldc;
+    g.path = path;
+    PCD_TRY(nn::gemm(g, (cudaStream_t)stream, partials));
+    if (path == 2) {
+        // the tensor-core form's bounded waits report through an error word
+        PCD_CUDA(cudaStreamSynchronize((cudaStream_t)stream));
+        int e = 0;
+        PCD_TRY(nn::gemm_tc_error(&e, true));
+        if (e) {
+            set_error("pcd_gemm_bf16_path: a bounded wait of the tcgen05 GEMM gave up");
+            return e;
+        }
+    }
+    return PCD_OK;
+}
+
 int pcd_ctx_set_warm_start_net(pcd_ctx *ctx, pcd_unet *u)
 {
     if (!ctx) return PCD_BAD_ARG;

@@ -33,6 +33,37 @@ def test_gemm_matches_torch(M, N, K, ksplit):
     assert err < 1e-5, err
 
 
+@pytest.mark.parametrize("M,N,K,ksplit", [(512, 128, 64, 1), (300, 96, 96, 1), (4096, 32, 288, 1), (1000, 256, 576, 2),
+                                          (130, 700, 160, 3), (8192, 64, 2304, 1), (16384, 128, 1152, 1)])
+def test_gemm_tcgen05_matches_torch(M, N, K, ksplit):
+    """The tcgen05 GEMM (TMA loads with the 128-byte swizzle, tcgen05.mma into
+    a tensor-memory accumulator, tcgen05.ld epilogue) against torch: tails in
+    M, N and K (K not a multiple of the 64-wide K tile, N below the N tile),
+    split-K, and the U-Net's convolution shapes; the mma.sync path on the same
+    inputs agrees too."""
+    import torch
+
+    from poisson_caustic_design_gb300 import _lib
+
+    L = _lib.load()
+    g = torch.Generator(device="cpu").manual_seed(M * 7 + N + K)
+    A = torch.randn(M, K, generator=g).to(torch.bfloat16).cuda()
+    B = torch.randn(N, K, generator=g).to(torch.bfloat16).cuda()
+    ref = A.float() @ B.float().T
+    out = {}
+    for path in (2, 1):
+        C = torch.full((M, N), float("nan"), dtype=torch.float32, device="cuda")
+        part = torch.zeros(ksplit * M * N, dtype=torch.float32, device="cuda")
+        st = L.pcd_gemm_bf16_path(A.data_ptr(), K, B.data_ptr(), K, C.data_ptr(), N, M, N, K, ksplit,
+                                  part.data_ptr(), path, torch.cuda.current_stream().cuda_stream)
+        assert st == 0, (path, L.pcd_last_error())
+        torch.cuda.synchronize()
+        out[path] = C
+        err = (C - ref).abs().max().item() / ref.abs().max().item()
+        assert err < 1e-5, (path, err)
+    assert (out[2] - out[1]).abs().max().item() <= 1e-5 * ref.abs().max().item()
+
+
 def torch_unet(params, x, bf16=False):
     """float32 CPU model of the library's U-Net with the flat parameters.
 
