@@ -323,10 +323,17 @@ int pcd_gemm_bf16(const void *A, int lda, const void *B, int ldb, float *C, int 
 /* The same GEMM on a chosen path: 0 automatic, 1 mma.sync (warp-level
  * tensor-core fragments through ldmatrix), 2 tcgen05 (TMA loads with the
  * 128-byte swizzle, tcgen05.mma into a tensor-memory accumulator; A and B
- * 16-byte aligned).  Path 2 synchronises `stream` and returns PCD_TIMEOUT if
- * a bounded wait of the kernel gave up.  No counterpart in the reference. */
+ * 16-byte aligned).  The tcgen05 kernel's bounded waits report through a
+ * device error word that pcd_gemm_bf16_status reads (after synchronising the
+ * device; PCD_TIMEOUT if a wait gave up since the last call) and clears.  No
+ * counterpart in the reference. */
 int pcd_gemm_bf16_path(const void *A, int lda, const void *B, int ldb, float *C, int ldc, int M, int N, int K,
                        int ksplit, float *partials, int path, void *stream);
+int pcd_gemm_bf16_status(void);
+/* What path 0 (automatic) means for every GEMM of the process, the U-Net's
+ * included: 0 (default) tcgen05 wherever it applies (16-byte aligned
+ * operands, K >= 64), else mma.sync; 1 mma.sync always. */
+int pcd_gemm_set_default_path(int path);
 /* network used by warm_start = PCD_WARM_LEARNED (not owned; NULL clears) */
 int pcd_ctx_set_warm_start_net(pcd_ctx *ctx, pcd_unet *net);
 

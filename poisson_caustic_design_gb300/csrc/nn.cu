@@ -16,6 +16,8 @@
 // second kernel in a fixed order.
 #include <cuda_bf16.h>
 
+#include <atomic>
+
 #include "nn.cuh"
 
 namespace pcd {
@@ -24,8 +26,11 @@ namespace nn {
 namespace {
 
 constexpr int GBM = 128, GBK = 32, GST = 3, GTHREADS = 256;
-// automatic path: the tcgen05 form for GEMMs it takes (nn_tc.cu)
-constexpr bool kTcAuto = false;
+// automatic path: the tcgen05 form (nn_tc.cu) for every GEMM it takes whose
+// output tiles fill the chip (a whole U-Net pass at 256^2 x 16: inference 7%
+// and a training step 13% faster than on mma.sync; at 64^2 x 1, where every
+// GEMM has 32 tiles or fewer, mma.sync is 13% faster), unless pinned to mma.sync
+std::atomic<int> g_default_path{0};
 constexpr int SROW = GBK + 8;  // padded shared row: 40 bf16 = 80 bytes
 
 __device__ __forceinline__ unsigned smem_u32(const void *p)
@@ -489,6 +494,16 @@ __global__ void k_slice_add(const float *in, long P, int C, float *out, int ld, 
 }  // namespace
 
 // ---------------------------------------------------------------------------
+int set_default_path(int path)
+{
+    if (path != 0 && path != 1) {
+        set_error("gemm default path must be 0 (tcgen05 where it applies) or 1 (mma.sync)");
+        return PCD_BAD_ARG;
+    }
+    g_default_path.store(path);
+    return PCD_OK;
+}
+
 size_t gemm_smem(int BN) { return (size_t)GST * (GBM + BN) * SROW * sizeof(__nv_bfloat16); }
 
 int gemm(const GemmArgs &g0, cudaStream_t s, float *partials)
@@ -513,7 +528,8 @@ int gemm(const GemmArgs &g0, cudaStream_t s, float *partials)
         g.Cb = nullptr;
         g.ldc = g.N;
     }
-    const bool tc = g.path == 2 || (g.path == 0 && kTcAuto && gemm_tc_applies(g));
+    const bool tc = g.path == 2 || (g.path == 0 && g_default_path.load() == 0 && gemm_tc_applies(g) &&
+                                    gemm_tc_fills_chip(g));
     const int BN = g.N <= 32 ? 32 : (g.N <= 64 ? 64 : 128);
     const dim3 grid((g.N + BN - 1) / BN, (g.M + GBM - 1) / GBM, g.ksplit);
     const size_t smem = gemm_smem(BN);

@@ -31,11 +31,24 @@ size_t gemm_smem(int BN);
 // partials: ksplit * M * N floats when ksplit > 1
 int gemm(const GemmArgs &g, cudaStream_t s, float *partials);
 // The tcgen05 form (nn_tc.cu): whether it takes g (16-byte aligned operands,
-// M of several 128-row tiles, K >= 64), the launch (split-K partials to
+// K >= 64), whether its output tiles fill the chip (at least one per SM; the
+// automatic choice takes it only then), the launch (split-K partials to
 // g.Cf), and the error word its bounded waits set (PCD_TIMEOUT).
 bool gemm_tc_applies(const GemmArgs &g);
+bool gemm_tc_fills_chip(const GemmArgs &g);
 int gemm_tc(const GemmArgs &g, cudaStream_t s);
 int gemm_tc_error(int *out, bool reset);
+// Everything the tcgen05 form sets up on first use (its error word, the
+// kernels' shared-memory attributes on the current device), done ahead so
+// that no allocation falls inside a stream capture; the error word itself.
+int gemm_tc_prepare();
+// Reads the current device's error word on stream s (synchronising it); a
+// nonzero word (a wait gave up, its tile left unwritten) is reset and
+// reported as PCD_DEVICE_ERROR.
+int gemm_tc_check(cudaStream_t s);
+// What path 0 means for the whole process: 0 tcgen05 where it applies, else
+// mma.sync; 1 mma.sync always.
+int set_default_path(int path);
 int im2col(const __nv_bfloat16 *in, int B, int H, int W, int C, int ldcin, __nv_bfloat16 *out, int Kp, cudaStream_t s);
 int transpose(const __nv_bfloat16 *in, int rows, int cols, int ldin, __nv_bfloat16 *out, int ldout, cudaStream_t s);
 int flip(const __nv_bfloat16 *Wt, int Cout, int Cin, int Kp, __nv_bfloat16 *Wf, int Kpf, cudaStream_t s);

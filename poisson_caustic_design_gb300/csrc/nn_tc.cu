@@ -117,6 +117,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     k_gemm_tc(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB, GemmArgs g, int *err)
 {
     static_assert(BN == 32 || BN == 64 || BN == 128 || BN == 256, "N tile");
+    static_assert(kTcBM * 33 * 4 <= kTcStages * (kTcBM * kTcBK * 2), "epilogue tile fits in the ring");
     constexpr unsigned kStageA = kTcBM * kTcBK * 2, kStageB = BN * kTcBK * 2, kStage = kStageA + kStageB;
     constexpr int kCols = BN < 32 ? 32 : BN;  // tensor memory columns (a power of 2, >= 32)
     extern __shared__ __align__(1024) unsigned char tc_buf[];
@@ -206,17 +207,22 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     }
     __syncthreads();
 
-    // ---- epilogue: warps 0-3, thread t <-> accumulator lane / tile row t
-    const bool fail = s_fail != 0 || nk == 0;
+    // ---- epilogue: 32 columns at a time, warp w reading accumulator lanes
+    // [32w, 32w + 32) (tile rows) with tcgen05.ld, through a shared tile in
+    // the (now idle) ring so that the stores of C run along its rows
+    const bool fail = s_fail != 0 || nk == 0;  // the same for every thread (read after a barrier)
+    bool lost = false;                         // the done wait ran out somewhere in the block
     if (!fail) {
-        if (!mbar_wait(done, 0u)) {
-            atomicCAS(err, 0, PCD_TIMEOUT);
-        } else {
+        // one decision for the whole block: every thread takes the same path
+        // through the barriers below
+        const bool ok = __syncthreads_and(mbar_wait(done, 0u)) != 0;
+        lost = !ok;
+        if (!ok && threadIdx.x == 0) atomicCAS(err, 0, PCD_TIMEOUT);
+        if (ok) {
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            const int row = bm + warp * 32 + lane;
-#pragma unroll
-            for (int c0 = 0; c0 < BN; c0 += 16) {
-                unsigned r[16];
+            float *tile = reinterpret_cast<float *>(tc_buf + (ring - raw));  // [128][33]
+            for (int c0 = 0; c0 < BN; c0 += 32) {
+                unsigned r[32];
                 const unsigned addr = tmem + ((unsigned)(warp * 32) << 16) + (unsigned)c0;
                 asm volatile(
                     "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
@@ -225,23 +231,34 @@ __global__ void __launch_bounds__(kTcThreads, 1)
                       "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
                       "=r"(r[15])
                     : "r"(addr));
+                asm volatile(
+                    "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
+                    "[%16];"
+                    : "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]),
+                      "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]),
+                      "=r"(r[30]), "=r"(r[31])
+                    : "r"(addr + 16u));
                 asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-                if (row < g.M) {
+                float *mine = tile + (warp * 32 + lane) * 33;
 #pragma unroll
-                    for (int j = 0; j < 16; j++) {
-                        const int n = bn + c0 + j;
-                        if (n >= g.N) continue;
-                        float v = __uint_as_float(r[j]);
-                        if (g.ksplit > 1) {
-                            g.Cf[((size_t)blockIdx.z * g.M + row) * g.ldc + n] = v;
-                            continue;
-                        }
-                        if (g.bias) v += g.bias[n];
-                        if (g.relu) v = fmaxf(v, 0.f);
-                        if (g.Cb) g.Cb[(size_t)row * g.ldc + n] = __float2bfloat16(v);
-                        else g.Cf[(size_t)row * g.ldc + n] = v;
+                for (int j = 0; j < 32; j++) mine[j] = __uint_as_float(r[j]);
+                __syncthreads();
+                const int n = bn + c0 + lane;
+                const float bias = (g.ksplit == 1 && g.bias && n < g.N) ? g.bias[n] : 0.f;
+                for (int rr = warp; rr < kTcBM; rr += kTcThreads / 32) {
+                    const int row = bm + rr;
+                    if (row >= g.M || n >= g.N) continue;
+                    float v = tile[rr * 33 + lane];
+                    if (g.ksplit > 1) {
+                        g.Cf[((size_t)blockIdx.z * g.M + row) * g.ldc + n] = v;
+                        continue;
                     }
+                    v += bias;
+                    if (g.relu) v = fmaxf(v, 0.f);
+                    if (g.Cb) g.Cb[(size_t)row * g.ldc + n] = __float2bfloat16(v);
+                    else g.Cf[(size_t)row * g.ldc + n] = v;
                 }
+                __syncthreads();
             }
         }
     } else if (nk == 0 && g.ksplit > 1) {
@@ -250,7 +267,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         if (row < g.M)
             for (int n = bn; n < min(g.N, bn + BN); n++) g.Cf[((size_t)blockIdx.z * g.M + row) * g.ldc + n] = 0.f;
     }
-    if (s_fail != 0 && threadIdx.x == 0) {
+    if ((s_fail != 0 || lost) && threadIdx.x == 0) {
         // let what is still in flight land before the shared memory and the
         // tensor memory go away: every MMA issued (one more commit), and each
         // stage's latest load (bounded waits)
@@ -307,20 +324,47 @@ int make_map(CUtensorMap *map, const void *base, int rows, int cols, int ld, int
     return PCD_OK;
 }
 
+// One error word per device: a kernel that gives up a bounded wait writes a
+// nonzero code there.
 int *err_word()
 {
-    static int *w = nullptr;
+    constexpr int kMaxDev = 64;
+    static int *w[kMaxDev] = {};
     static std::mutex mu;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDev) return nullptr;
     std::lock_guard<std::mutex> lk(mu);
-    if (!w && cudaMalloc(&w, sizeof(int)) == cudaSuccess) cudaMemset(w, 0, sizeof(int));
-    return w;
+    if (!w[dev] && cudaMalloc(&w[dev], sizeof(int)) == cudaSuccess) cudaMemset(w[dev], 0, sizeof(int));
+    return w[dev];
+}
+
+template <int BN>
+constexpr size_t tc_smem_bytes()
+{
+    return (size_t)kTcStages * (kTcBM * kTcBK * 2 + BN * kTcBK * 2) + 1024;
+}
+
+// The kernel's shared-memory attribute, set on the current device the first
+// time (the setting belongs to the function on that device).
+template <int BN>
+int tc_attr()
+{
+    static std::mutex mu;
+    static unsigned long long done_mask = 0;
+    int dev = 0;
+    PCD_CUDA(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lk(mu);
+    if (dev < 64 && (done_mask >> dev & 1ull)) return PCD_OK;
+    PCD_CUDA(cudaFuncSetAttribute(k_gemm_tc<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tc_smem_bytes<BN>()));
+    if (dev < 64) done_mask |= 1ull << dev;
+    return PCD_OK;
 }
 
 template <int BN>
 int launch_tc(const CUtensorMap &ma, const CUtensorMap &mb, const GemmArgs &g, cudaStream_t s, int *err)
 {
-    const size_t smem = (size_t)kTcStages * (kTcBM * kTcBK * 2 + BN * kTcBK * 2) + 1024;
-    PCD_CUDA(cudaFuncSetAttribute(k_gemm_tc<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const size_t smem = tc_smem_bytes<BN>();
+    PCD_TRY(tc_attr<BN>());
     const dim3 grid((g.N + BN - 1) / BN, (g.M + kTcBM - 1) / kTcBM, g.ksplit);
     k_gemm_tc<BN><<<grid, kTcThreads, smem, s>>>(ma, mb, g, err);
     PCD_LAUNCHED(1);
@@ -332,14 +376,35 @@ int launch_tc(const CUtensorMap &ma, const CUtensorMap &mb, const GemmArgs &g, c
 bool gemm_tc_applies(const GemmArgs &g)
 {
     // TMA: 16-byte aligned bases and row strides (ld multiples of 8, checked
-    // by gemm); the tensor-core tile only pays for itself on large M
-    return ((uintptr_t)g.A % 16) == 0 && ((uintptr_t)g.B % 16) == 0 && g.M >= 4 * kTcBM && g.K >= kTcBK;
+    // by gemm); at least one 64-wide K tile
+    return ((uintptr_t)g.A % 16) == 0 && ((uintptr_t)g.B % 16) == 0 && g.K >= kTcBK;
+}
+
+static int tc_bn(int N) { return N <= 32 ? 32 : (N <= 64 ? 64 : (N <= 128 ? 128 : 256)); }
+
+bool gemm_tc_fills_chip(const GemmArgs &g)
+{
+    // Below one CTA per SM the per-CTA set-up (tensor-memory allocation,
+    // barrier initialisation, the tensor maps' fetch) and the single issuing
+    // thread's latency are not hidden: at 64^2 pixels and batch 1 the U-Net's
+    // GEMMs (32 tiles and fewer) run faster on the mma.sync kernel.
+    static int sms = 0;
+    if (!sms) {
+        int dev = 0, n = 0;
+        if (cudaGetDevice(&dev) == cudaSuccess &&
+            cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess && n > 0)
+            sms = n;
+        else
+            return false;
+    }
+    const long tiles = (long)((g.M + kTcBM - 1) / kTcBM) * ((g.N + tc_bn(g.N) - 1) / tc_bn(g.N)) * g.ksplit;
+    return tiles >= sms;
 }
 
 int gemm_tc(const GemmArgs &g, cudaStream_t s)
 {
     CUtensorMap ma, mb;
-    const int BN = g.N <= 32 ? 32 : (g.N <= 64 ? 64 : 128);
+    const int BN = tc_bn(g.N);
     PCD_TRY(make_map(&ma, g.A, g.M, g.K, g.lda, kTcBM));
     PCD_TRY(make_map(&mb, g.B, g.N, g.K, g.ldb, BN));
     int *err = err_word();
@@ -349,13 +414,51 @@ int gemm_tc(const GemmArgs &g, cudaStream_t s)
     }
     if (BN == 32) return launch_tc<32>(ma, mb, g, s, err);
     if (BN == 64) return launch_tc<64>(ma, mb, g, s, err);
-    return launch_tc<128>(ma, mb, g, s, err);
+    if (BN == 128) return launch_tc<128>(ma, mb, g, s, err);
+    return launch_tc<256>(ma, mb, g, s, err);
+}
+
+int gemm_tc_prepare()
+{
+    if (!err_word()) {
+        set_error("tcgen05 gemm: no error word");
+        return PCD_DEVICE_ERROR;
+    }
+    PCD_TRY(tc_attr<32>());
+    PCD_TRY(tc_attr<64>());
+    PCD_TRY(tc_attr<128>());
+    PCD_TRY(tc_attr<256>());
+    if (!encode_fn()) {
+        set_error("tcgen05 gemm: cuTensorMapEncodeTiled is not available");
+        return PCD_DEVICE_ERROR;
+    }
+    return PCD_OK;
+}
+
+int gemm_tc_check(cudaStream_t s)
+{
+    int *w = err_word();
+    if (!w) {
+        set_error("tcgen05 gemm: no error word");
+        return PCD_DEVICE_ERROR;
+    }
+    int v = 0;
+    PCD_CUDA(cudaMemcpyAsync(&v, w, sizeof(int), cudaMemcpyDeviceToHost, s));
+    PCD_CUDA(cudaStreamSynchronize(s));
+    if (v != 0) {
+        PCD_CUDA(cudaMemsetAsync(w, 0, sizeof(int), s));
+        PCD_CUDA(cudaStreamSynchronize(s));
+        set_error("tcgen05 gemm: a pipeline wait gave up (code " + std::to_string(v) + ")");
+        return PCD_DEVICE_ERROR;
+    }
+    return PCD_OK;
 }
 
 int gemm_tc_error(int *out, bool reset)
 {
     int *w = err_word();
     if (!w) return PCD_DEVICE_ERROR;
+    PCD_CUDA(cudaDeviceSynchronize());
     PCD_CUDA(cudaMemcpy(out, w, sizeof(int), cudaMemcpyDeviceToHost));
     if (reset) PCD_CUDA(cudaMemset(w, 0, sizeof(int)));
     return PCD_OK;

@@ -480,6 +480,9 @@ int UNet::train_step(const float *x, const float *target, int B, const nn::AdamP
         std::vector<float> lp(np);
         PCD_CUDA(cudaMemcpyAsync(lp.data(), lossbuf + 64, np * sizeof(float), cudaMemcpyDeviceToHost, s));
         PCD_CUDA(cudaStreamSynchronize(s));
+        // the step already waits for the loss: the tensor-core GEMMs' wait
+        // status costs one more 4-byte copy here
+        PCD_TRY(nn::gemm_tc_check(s));
         double t = 0.0;
         for (float f : lp) t += f;
         *loss = (float)t;
@@ -538,6 +541,9 @@ int pcd_unet_create(pcd_ctx *ctx, int resolution, int max_batch, unsigned long l
     u->ctx = ctx;
     int st = u->net.build(resolution, max_batch);
     if (st == PCD_OK) st = u->net.init_random(seed);
+    // the tensor-core GEMM's set-up before any use of the network inside a
+    // stream capture (the learned warm start's judge graph)
+    if (st == PCD_OK) st = nn::gemm_tc_prepare();
     if (st != PCD_OK) {
         delete u;
         return st;
@@ -691,16 +697,18 @@ int pcd_gemm_bf16_path(const void *A, int lda, const void *B, int ldb, float *C,
     g.Cf = C;
     g.ldc = ldc;
     g.path = path;
-    PCD_TRY(nn::gemm(g, (cudaStream_t)stream, partials));
-    if (path == 2) {
-        // the tensor-core form's bounded waits report through an error word
-        PCD_CUDA(cudaStreamSynchronize((cudaStream_t)stream));
-        int e = 0;
-        PCD_TRY(nn::gemm_tc_error(&e, true));
-        if (e) {
-            set_error("pcd_gemm_bf16_path: a bounded wait of the tcgen05 GEMM gave up");
-            return e;
-        }
+    return nn::gemm(g, (cudaStream_t)stream, partials);
+}
+
+int pcd_gemm_set_default_path(int path) { return nn::set_default_path(path); }
+
+int pcd_gemm_bf16_status(void)
+{
+    int e = 0;
+    PCD_TRY(nn::gemm_tc_error(&e, true));
+    if (e) {
+        set_error("a bounded wait of the tcgen05 GEMM gave up");
+        return e;
     }
     return PCD_OK;
 }

@@ -435,7 +435,7 @@ def test_design_members_pixels_gradient_and_cells(ctx, port):
     (caustic_design.cpp:335), gradient = calculate_gradient(phi) (the port's,
     bit for bit), and target_cells = the barycentric dual cells the last
     transport iteration was built from, whose shoelace areas are the areas
-    behind that iteration's errors (target / (1 + error))."""
+    behind that iteration's errors (area * (1 + error) = target)."""
     z = load_golden("pipeline_r16.npz")
     d, _ = _design(ctx, z)
     assert np.array_equal(d.pixels, port.scale_proportional(z["image"], 0.0, 1.0))
@@ -451,8 +451,9 @@ def test_design_members_pixels_gradient_and_cells(ctx, port):
         x, y = q[:, 0], q[:, 1]
         return 0.5 * np.sum(x * np.roll(y, -1) - np.roll(x, -1) * y)
 
+    # errors = (target - area) / area (caustic_design.cpp:202-209); a black
+    # pixel's target area is 0 and its error exactly -1, so compare products
     areas = np.array([sum(shoelace(q) for q in c) for c in cells])
-    expect = d.target_areas / (1.0 + d.errors)
-    np.testing.assert_allclose(areas, expect, rtol=1e-12)
+    np.testing.assert_allclose(areas * (1.0 + d.errors), d.target_areas, rtol=1e-10, atol=1e-12 * areas.max())
     assert d.first_target_cells == []
     d.close()

@@ -34,7 +34,8 @@ def test_gemm_matches_torch(M, N, K, ksplit):
 
 
 @pytest.mark.parametrize("M,N,K,ksplit", [(512, 128, 64, 1), (300, 96, 96, 1), (4096, 32, 288, 1), (1000, 256, 576, 2),
-                                          (130, 700, 160, 3), (8192, 64, 2304, 1), (16384, 128, 1152, 1)])
+                                          (130, 700, 160, 3), (8192, 64, 2304, 1), (16384, 128, 1152, 1),
+                                          (2048, 256, 2304, 1), (700, 300, 192, 2)])
 def test_gemm_tcgen05_matches_torch(M, N, K, ksplit):
     """The tcgen05 GEMM (TMA loads with the 128-byte swizzle, tcgen05.mma into
     a tensor-memory accumulator, tcgen05.ld epilogue) against torch: tails in
@@ -58,6 +59,7 @@ def test_gemm_tcgen05_matches_torch(M, N, K, ksplit):
                                   part.data_ptr(), path, torch.cuda.current_stream().cuda_stream)
         assert st == 0, (path, L.pcd_last_error())
         torch.cuda.synchronize()
+        assert L.pcd_gemm_bf16_status() == 0, L.pcd_last_error()
         out[path] = C
         err = (C - ref).abs().max().item() / ref.abs().max().item()
         assert err < 1e-5, (path, err)
