@@ -330,6 +330,14 @@ int pcd_gemm_bf16(const void *A, int lda, const void *B, int ldb, float *C, int 
 int pcd_gemm_bf16_path(const void *A, int lda, const void *B, int ldb, float *C, int ldc, int M, int N, int K,
                        int ksplit, float *partials, int path, void *stream);
 int pcd_gemm_bf16_status(void);
+/* The tcgen05 GEMM with operand layouts: a_mn = 1 gives A as K rows of M
+ * (A^T stored row-major, [K][M] with row stride lda), b_mn = 1 gives B as
+ * [K][N] (row stride ldb), trans_c = 1 stores C transposed (C[n][m] at
+ * n * ldc + m).  MN-major extents of at least 64 (32 for B with N <= 32),
+ * K >= 64 and any K; the U-Net's weight gradient dW^T = col^T dY is this
+ * form.  No counterpart in the reference. */
+int pcd_gemm_bf16_layout(const void *A, int lda, int a_mn, const void *B, int ldb, int b_mn, float *C, int ldc,
+                         int trans_c, int M, int N, int K, int ksplit, float *partials, void *stream);
 /* What path 0 (automatic) means for every GEMM of the process, the U-Net's
  * included: 0 (default) tcgen05 wherever it applies (16-byte aligned
  * operands, K >= 64), else mma.sync; 1 mma.sync always. */

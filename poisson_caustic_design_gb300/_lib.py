@@ -172,6 +172,8 @@ SIGNATURES = {
     "pcd_gemm_bf16_path": (C.c_int, [_vp, C.c_int, _vp, C.c_int, _vp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
                                      _vp, C.c_int, _vp]),
     "pcd_gemm_bf16_status": (C.c_int, []),
+    "pcd_gemm_bf16_layout": (C.c_int, [_vp, C.c_int, C.c_int, _vp, C.c_int, C.c_int, _vp, C.c_int, C.c_int, C.c_int,
+                                       C.c_int, C.c_int, C.c_int, _vp, _vp]),
     "pcd_gemm_set_default_path": (C.c_int, [C.c_int]),
     "pcd_design_params_default": (C.c_int, [C.POINTER(DesignParams)]),
     "pcd_design_create": (C.c_int, [_vp, C.POINTER(DesignParams), C.POINTER(_vp)]),

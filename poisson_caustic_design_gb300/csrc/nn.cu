@@ -504,12 +504,24 @@ int set_default_path(int path)
     return PCD_OK;
 }
 
+int default_path() { return g_default_path.load(); }
+
 size_t gemm_smem(int BN) { return (size_t)GST * (GBM + BN) * SROW * sizeof(__nv_bfloat16); }
 
 int gemm(const GemmArgs &g0, cudaStream_t s, float *partials)
 {
     GemmArgs g = g0;
-    if (g.K % GBK != 0 || g.lda % 8 || g.ldb % 8 || g.M < 1 || g.N < 1) {
+    const bool layout_tc = g.a_mn || g.b_mn || g.trans_c;  // forms only the tcgen05 kernel has
+    if (layout_tc) {
+        if (g.path == 1 || !gemm_tc_applies(g) || g.lda % 8 || g.ldb % 8 || g.M < 1 || g.N < 1 ||
+            (g.trans_c && (g.Cb || g.bias || g.relu || !g.Cf))) {
+            set_error("nn gemm: MN-major operands and a transposed C need the tcgen05 path (aligned operands, "
+                      "K >= 64, MN-major extents >= 64, FP32 C without bias or ReLU)");
+            return PCD_BAD_ARG;
+        }
+        g.path = 2;
+    }
+    if ((!layout_tc && g.K % GBK != 0) || g.lda % 8 || g.ldb % 8 || g.M < 1 || g.N < 1) {
         set_error("nn gemm: K must be a multiple of 32 and leading dimensions multiples of 8");
         return PCD_BAD_ARG;
     }
@@ -526,7 +538,7 @@ int gemm(const GemmArgs &g0, cudaStream_t s, float *partials)
         }
         g.Cf = partials;
         g.Cb = nullptr;
-        g.ldc = g.N;
+        g.ldc = g.trans_c ? g.M : g.N;  // partials as [split][M][N], or [split][N][M] for a transposed C
     }
     const bool tc = g.path == 2 || (g.path == 0 && g_default_path.load() == 0 && gemm_tc_applies(g) &&
                                     gemm_tc_fills_chip(g));
@@ -550,7 +562,12 @@ int gemm(const GemmArgs &g0, cudaStream_t s, float *partials)
         k_gemm<128><<<grid, GTHREADS, smem, s>>>(g);
     }
     if (!tc) PCD_LAUNCHED(1);
-    if (g.ksplit > 1) {
+    if (g.ksplit > 1 && g.trans_c) {
+        // the transposed partials reduce as an N x M matrix into C[n][m]
+        k_splitk_reduce<<<grid1d((long)g.M * g.N), 256, 0, s>>>(partials, g.ksplit, g.N, g.M, g.M, nullptr, 0, nullptr,
+                                                               outF, ldo);
+        PCD_LAUNCHED(1);
+    } else if (g.ksplit > 1) {
         k_splitk_reduce<<<grid1d((long)g.M * g.N), 256, 0, s>>>(partials, g.ksplit, g.M, g.N, g.N, g.bias, g.relu,
                                                                outB, outF, ldo);
         PCD_LAUNCHED(1);

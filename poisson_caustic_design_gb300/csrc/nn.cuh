@@ -21,6 +21,10 @@ struct GemmArgs {
     float *Cf;               // FP32 output
     int ldc;
     int path = 0;            // 0 automatic, 1 mma.sync, 2 tcgen05 (TMA + tensor memory)
+    // tcgen05 only: an operand stored K-rows x M (or N) contiguous ("MN-major",
+    // e.g. A given as [K][M] with row stride lda), and C stored transposed
+    // (C[n][m] at n * ldc + m; FP32 only, no bias or ReLU)
+    int a_mn = 0, b_mn = 0, trans_c = 0;
 };
 
 struct AdamParams {
@@ -49,6 +53,7 @@ int gemm_tc_check(cudaStream_t s);
 // What path 0 means for the whole process: 0 tcgen05 where it applies, else
 // mma.sync; 1 mma.sync always.
 int set_default_path(int path);
+int default_path();
 int im2col(const __nv_bfloat16 *in, int B, int H, int W, int C, int ldcin, __nv_bfloat16 *out, int Kp, cudaStream_t s);
 int transpose(const __nv_bfloat16 *in, int rows, int cols, int ldin, __nv_bfloat16 *out, int ldout, cudaStream_t s);
 int flip(const __nv_bfloat16 *Wt, int Cout, int Cin, int Kp, __nv_bfloat16 *Wf, int Kpf, cudaStream_t s);

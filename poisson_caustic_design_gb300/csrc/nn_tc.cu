@@ -78,22 +78,63 @@ __device__ __forceinline__ void tma_load_2d(unsigned dst, const CUtensorMap *map
         : "memory");
 }
 
-// Shared memory descriptor of a K-major operand tile with the 128-byte
-// swizzle: rows of 128 bytes (64 BF16 of K), 8-row swizzle atoms 1024 bytes
-// apart (stride byte offset), leading byte offset unused for this layout
-// (encoded 1), descriptor version 1 (bits 46-47), swizzle mode 2 (bits 61-63).
-__device__ __forceinline__ unsigned long long smem_desc_sw128(unsigned addr)
+// Shared memory descriptor: start address >> 4 (bits 0-13), leading byte
+// offset >> 4 (bits 16-29), stride byte offset >> 4 (bits 32-45), descriptor
+// version 1 (bits 46-47), swizzle mode (bits 61-63: 2 = 128-byte, 4 = 64-byte).
+__device__ __forceinline__ unsigned long long smem_desc(unsigned addr, unsigned lbo, unsigned sbo, unsigned mode)
 {
-    return (unsigned long long)((addr & 0x3FFFFu) >> 4) | (1ull << 16) | ((unsigned long long)(1024 >> 4) << 32) |
-           (1ull << 46) | (2ull << 61);
+    return (unsigned long long)((addr & 0x3FFFFu) >> 4) | ((unsigned long long)((lbo >> 4) & 0x3FFFu) << 16) |
+           ((unsigned long long)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46) | ((unsigned long long)mode << 61);
+}
+
+// Operand tiles as TMA lays them down with the 128-byte swizzle (and, for a
+// 32-wide MN-major tile, the 64-byte swizzle), and the descriptor of the
+// 16-deep K slice kk:
+//   K-major: rows of 64 K values (128 bytes), 8-row atoms 1024 bytes apart
+//     (stride offset); the leading offset is unused for this layout (encoded
+//     1); slice kk starts 32 bytes further inside the atom;
+//   MN-major: rows of 64 M (or N) values, one row per K index; 8-row atoms
+//     along K 1024 bytes apart (stride offset), 64-wide MN blocks of 64 rows
+//     8192 bytes apart (leading offset); slice kk starts 16 rows (2048 bytes)
+//     further.  32-wide (64-byte swizzle): 512-byte atoms, 1024 bytes a slice.
+__device__ __forceinline__ unsigned long long desc_kmajor(unsigned tile, int kk)
+{
+    return smem_desc(tile + 32u * kk, 16u, 1024u, 2u);
+}
+
+__device__ __forceinline__ unsigned long long desc_mnmajor(unsigned tile, int kk, int width)
+{
+    return width == 32 ? smem_desc(tile + 1024u * kk, 4096u, 512u, 4u) : smem_desc(tile + 2048u * kk, 8192u, 1024u, 2u);
 }
 
 // Instruction descriptor of kind::f16: D FP32 (bits 4-5 = 1), A and B BF16
-// (bits 7-9 = 1, 10-12 = 1), both K-major (bits 15, 16 = 0), N >> 3 in bits
-// 17-22, M >> 4 in bits 24-28.
-__host__ __device__ constexpr unsigned idesc_bf16_f32(int M, int N)
+// (bits 7-9 = 1, 10-12 = 1), A and B major-ness (bits 15, 16: 0 K-major,
+// 1 MN-major), N >> 3 in bits 17-22, M >> 4 in bits 24-28.
+__host__ __device__ constexpr unsigned idesc_bf16_f32(int M, int N, int a_mn = 0, int b_mn = 0)
 {
-    return (1u << 4) | (1u << 7) | (1u << 10) | ((unsigned)(N >> 3) << 17) | ((unsigned)(M >> 4) << 24);
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((unsigned)a_mn << 15) | ((unsigned)b_mn << 16) |
+           ((unsigned)(N >> 3) << 17) | ((unsigned)(M >> 4) << 24);
+}
+
+// One stage's loads: A (128 rows of M) and B (BN rows of N) for K tile k0.
+// A K-major operand is one box of 64 K columns; an MN-major operand is one
+// box of 64 K rows per 64 (or 32) columns of M / N, 8192 bytes apart.
+template <int BN>
+__device__ __forceinline__ void load_stage(unsigned st, unsigned stB, const CUtensorMap *mA, const CUtensorMap *mB,
+                                           unsigned bar, const GemmArgs &g, int k0, int bm, int bn)
+{
+    if (g.a_mn) {
+        tma_load_2d(st, mA, bar, bm, k0);
+        tma_load_2d(st + 8192u, mA, bar, bm + 64, k0);
+    } else {
+        tma_load_2d(st, mA, bar, k0, bm);
+    }
+    if (g.b_mn) {
+#pragma unroll
+        for (int c = 0; c < (BN < 64 ? 1 : BN / 64); c++) tma_load_2d(stB + 8192u * c, mB, bar, bn + 64 * c, k0);
+    } else {
+        tma_load_2d(stB, mB, bar, k0, bn);
+    }
 }
 
 __device__ __forceinline__ void mma_bf16_tc(unsigned tmem_d, unsigned long long a, unsigned long long b, unsigned idesc,
@@ -163,14 +204,13 @@ __global__ void __launch_bounds__(kTcThreads, 1)
 
     // ---- producer + MMA issuer: thread 0
     if (threadIdx.x == 0 && nk > 0) {
-        constexpr unsigned idesc = idesc_bf16_f32(kTcBM, BN);
+        const unsigned idesc = idesc_bf16_f32(kTcBM, BN, g.a_mn, g.b_mn);
         bool ok = true;
         const int pre = min(nk, kTcStages);
         for (int i = 0; i < pre; i++) {
             const unsigned st = ring + (unsigned)i * kStage;
             mbar_expect_tx(full0 + 8 * i, kStage);
-            tma_load_2d(st, &mapA, full0 + 8 * i, (kt0 + i) * kTcBK, bm);
-            tma_load_2d(st + kStageA, &mapB, full0 + 8 * i, (kt0 + i) * kTcBK, bn);
+            load_stage<BN>(st, st + kStageA, &mapA, &mapB, full0 + 8 * i, g, (kt0 + i) * kTcBK, bm, bn);
             s_fills[i]++;
         }
         int issued = pre;
@@ -182,7 +222,8 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             const unsigned a = ring + (unsigned)s * kStage, b = a + kStageA;
 #pragma unroll
             for (int kk = 0; kk < kTcBK / 16; kk++)
-                mma_bf16_tc(tmem, smem_desc_sw128(a + 32u * kk), smem_desc_sw128(b + 32u * kk), idesc,
+                mma_bf16_tc(tmem, g.a_mn ? desc_mnmajor(a, kk, 64) : desc_kmajor(a, kk),
+                            g.b_mn ? desc_mnmajor(b, kk, BN < 64 ? BN : 64) : desc_kmajor(b, kk), idesc,
                             (i > 0 || kk > 0) ? 1u : 0u);
             mma_commit(empty0 + 8 * s);
             // refill the stage of the previous K tile once its MMAs are done
@@ -192,8 +233,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
                 if (!mbar_wait(empty0 + 8 * ps, pphase)) { ok = false; break; }
                 const unsigned st = ring + (unsigned)ps * kStage;
                 mbar_expect_tx(full0 + 8 * ps, kStage);
-                tma_load_2d(st, &mapA, full0 + 8 * ps, (kt0 + issued) * kTcBK, bm);
-                tma_load_2d(st + kStageA, &mapB, full0 + 8 * ps, (kt0 + issued) * kTcBK, bn);
+                load_stage<BN>(st, st + kStageA, &mapA, &mapB, full0 + 8 * ps, g, (kt0 + issued) * kTcBK, bm, bn);
                 s_fills[ps]++;
                 issued++;
             }
@@ -239,6 +279,21 @@ __global__ void __launch_bounds__(kTcThreads, 1)
                       "=r"(r[30]), "=r"(r[31])
                     : "r"(addr + 16u));
                 asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+                if (g.trans_c) {
+                    // C[n][m]: a warp's 32 lanes are 32 consecutive m, so each
+                    // column n is one 128-byte store (split-K partials as
+                    // [split][N][M], ldc = M)
+                    const int m = bm + warp * 32 + lane;
+                    if (m < g.M) {
+                        float *base = g.Cf + (g.ksplit > 1 ? (size_t)blockIdx.z * g.N * g.ldc : 0);
+#pragma unroll
+                        for (int j = 0; j < 32; j++) {
+                            const int n = bn + c0 + j;
+                            if (n < g.N) base[(size_t)n * g.ldc + m] = __uint_as_float(r[j]);
+                        }
+                    }
+                    continue;
+                }
                 float *mine = tile + (warp * 32 + lane) * 33;
 #pragma unroll
                 for (int j = 0; j < 32; j++) mine[j] = __uint_as_float(r[j]);
@@ -265,7 +320,10 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         // an empty K share still writes zero partials
         const int row = bm + warp * 32 + lane;
         if (row < g.M)
-            for (int n = bn; n < min(g.N, bn + BN); n++) g.Cf[((size_t)blockIdx.z * g.M + row) * g.ldc + n] = 0.f;
+            for (int n = bn; n < min(g.N, bn + BN); n++) {
+                if (g.trans_c) g.Cf[((size_t)blockIdx.z * g.N + n) * g.ldc + row] = 0.f;
+                else g.Cf[((size_t)blockIdx.z * g.M + row) * g.ldc + n] = 0.f;
+            }
     }
     if ((s_fail != 0 || lost) && threadIdx.x == 0) {
         // let what is still in flight land before the shared memory and the
@@ -302,8 +360,9 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_fn()
 }
 
 // A 2-D tensor map of a rows x cols BF16 matrix (row stride ld elements) with
-// box rows x 64 columns and the 128-byte swizzle.
-int make_map(CUtensorMap *map, const void *base, int rows, int cols, int ld, int box_rows)
+// a box of box_rows x box_cols (box_cols of 64: the 128-byte swizzle; of 32:
+// the 64-byte swizzle).
+int make_map(CUtensorMap *map, const void *base, int rows, int cols, int ld, int box_rows, int box_cols = kTcBK)
 {
     auto fn = encode_fn();
     if (!fn) {
@@ -312,10 +371,12 @@ int make_map(CUtensorMap *map, const void *base, int rows, int cols, int ld, int
     }
     const cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
     const cuuint64_t strides[1] = {(cuuint64_t)ld * 2};
-    const cuuint32_t box[2] = {(cuuint32_t)kTcBK, (cuuint32_t)box_rows};
+    const cuuint32_t box[2] = {(cuuint32_t)box_cols, (cuuint32_t)box_rows};
     const cuuint32_t estr[2] = {1, 1};
     const CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void *>(base), dims, strides, box, estr,
-                          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                          CU_TENSOR_MAP_INTERLEAVE_NONE,
+                          box_cols == 32 ? CU_TENSOR_MAP_SWIZZLE_64B : CU_TENSOR_MAP_SWIZZLE_128B,
+                          CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                           CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) {
         set_error("tcgen05 gemm: cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")");
@@ -376,7 +437,10 @@ int launch_tc(const CUtensorMap &ma, const CUtensorMap &mb, const GemmArgs &g, c
 bool gemm_tc_applies(const GemmArgs &g)
 {
     // TMA: 16-byte aligned bases and row strides (ld multiples of 8, checked
-    // by gemm); at least one 64-wide K tile
+    // by gemm); at least one 64-wide K tile; an MN-major operand at least as
+    // wide as its box (64 columns; 32 for a 32-wide B)
+    if (g.a_mn && g.M < 64) return false;
+    if (g.b_mn && g.N < (g.N <= 32 ? 32 : 64)) return false;
     return ((uintptr_t)g.A % 16) == 0 && ((uintptr_t)g.B % 16) == 0 && g.K >= kTcBK;
 }
 
@@ -405,8 +469,10 @@ int gemm_tc(const GemmArgs &g, cudaStream_t s)
 {
     CUtensorMap ma, mb;
     const int BN = tc_bn(g.N);
-    PCD_TRY(make_map(&ma, g.A, g.M, g.K, g.lda, kTcBM));
-    PCD_TRY(make_map(&mb, g.B, g.N, g.K, g.ldb, BN));
+    if (g.a_mn) PCD_TRY(make_map(&ma, g.A, g.K, g.M, g.lda, kTcBK, 64));
+    else PCD_TRY(make_map(&ma, g.A, g.M, g.K, g.lda, kTcBM));
+    if (g.b_mn) PCD_TRY(make_map(&mb, g.B, g.K, g.N, g.ldb, kTcBK, BN < 64 ? BN : 64));
+    else PCD_TRY(make_map(&mb, g.B, g.N, g.K, g.ldb, BN));
     int *err = err_word();
     if (!err) {
         set_error("tcgen05 gemm: no error word");

@@ -371,19 +371,46 @@ int UNet::conv_bwd(Conv &c, int B, const float *dY, int lddy, float *dX, cudaStr
     float *gw = params_f + nparams + c.off_w, *gb = params_f + nparams + c.off_b;
     PCD_TRY(nn::relu_bwd(dY, lddy, c.out, c.ldout, P, c.Cout, c.relu, dym, s));
     PCD_TRY(nn::colsum(dym, P, c.Cout, colpart, gb, s));
-    // dW[Cout][Kp] = dYm^T (Cout x P) * col (P x Kp): both operands transposed to K = P contiguous
-    PCD_TRY(nn::transpose(dym, (int)P, c.Cout, c.Cout, tr_a, (int)P, s));
-    PCD_TRY(nn::transpose(c.col, (int)P, c.Kp, c.Kp, tr_b, (int)P, s));
     nn::GemmArgs g{};
-    g.A = tr_a;
-    g.lda = (int)P;
-    g.B = tr_b;
-    g.ldb = (int)P;
-    g.M = c.Cout;
-    g.N = c.Kp;
-    g.K = (int)P;
-    const int tiles = ((c.Kp + 127) / 128) * ((c.Cout + 127) / 128);
-    g.ksplit = std::max(1, std::min(32, 1216 / tiles));
+    // dW^T[Kp][Cout] = col^T (Kp x P) * dYm (P x Cout) on the tcgen05 kernel,
+    // both operands read where they lie (MN-major: col is [P][Kp], dYm
+    // [P][Cout]) and the result stored transposed into dW[Cout][Kp]; K = P
+    // split so that about two CTAs per SM share it
+    nn::GemmArgs mn{};
+    mn.A = c.col;
+    mn.lda = c.Kp;
+    mn.a_mn = 1;
+    mn.B = dym;
+    mn.ldb = c.Cout;
+    mn.b_mn = 1;
+    mn.M = c.Kp;
+    mn.N = c.Cout;
+    mn.K = (int)P;
+    mn.trans_c = 1;
+    if (nn::default_path() == 0 && nn::gemm_tc_applies(mn)) {
+        g = mn;
+        const int bn = c.Cout <= 32 ? 32 : (c.Cout <= 64 ? 64 : (c.Cout <= 128 ? 128 : 256));
+        const long tiles = (long)((c.Kp + 127) / 128) * ((c.Cout + bn - 1) / bn);
+        int dev = 0, sms = 148;
+        if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        const long kt = (P + 63) / 64;
+        g.ksplit = (int)std::max<long>(1, std::min<long>(std::min<long>((2L * sms + tiles - 1) / tiles, kt), 128));
+        while (g.ksplit > 1 && (size_t)g.ksplit * g.M * g.N > partials_cap) g.ksplit /= 2;
+    } else {
+        // dW[Cout][Kp] = dYm^T (Cout x P) * col (P x Kp): both operands
+        // transposed to K = P contiguous for the mma.sync kernel
+        PCD_TRY(nn::transpose(dym, (int)P, c.Cout, c.Cout, tr_a, (int)P, s));
+        PCD_TRY(nn::transpose(c.col, (int)P, c.Kp, c.Kp, tr_b, (int)P, s));
+        g.A = tr_a;
+        g.lda = (int)P;
+        g.B = tr_b;
+        g.ldb = (int)P;
+        g.M = c.Cout;
+        g.N = c.Kp;
+        g.K = (int)P;
+        const int tiles = ((c.Kp + 127) / 128) * ((c.Cout + 127) / 128);
+        g.ksplit = std::max(1, std::min(32, 1216 / tiles));
+    }
     g.Cf = gw;
     g.ldc = c.Kp;
     PCD_TRY(nn::gemm(g, s, partials));
@@ -697,6 +724,27 @@ int pcd_gemm_bf16_path(const void *A, int lda, const void *B, int ldb, float *C,
     g.Cf = C;
     g.ldc = ldc;
     g.path = path;
+    return nn::gemm(g, (cudaStream_t)stream, partials);
+}
+
+int pcd_gemm_bf16_layout(const void *A, int lda, int a_mn, const void *B, int ldb, int b_mn, float *C, int ldc,
+                         int trans_c, int M, int N, int K, int ksplit, float *partials, void *stream)
+{
+    nn::GemmArgs g{};
+    g.A = (const __nv_bfloat16 *)A;
+    g.lda = lda;
+    g.B = (const __nv_bfloat16 *)B;
+    g.ldb = ldb;
+    g.M = M;
+    g.N = N;
+    g.K = K;
+    g.ksplit = ksplit;
+    g.Cf = C;
+    g.ldc = ldc;
+    g.path = 2;
+    g.a_mn = a_mn != 0;
+    g.b_mn = b_mn != 0;
+    g.trans_c = trans_c != 0;
     return nn::gemm(g, (cudaStream_t)stream, partials);
 }
 

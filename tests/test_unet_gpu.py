@@ -66,6 +66,44 @@ def test_gemm_tcgen05_matches_torch(M, N, K, ksplit):
     assert (out[2] - out[1]).abs().max().item() <= 1e-5 * ref.abs().max().item()
 
 
+@pytest.mark.parametrize("M,N,K,ksplit,a_mn,b_mn,trans_c",
+                         [(288, 32, 4096, 8, 1, 1, 1), (576, 64, 3000, 4, 1, 1, 1), (1152, 128, 2048, 1, 1, 1, 1),
+                          (3456, 128, 1000, 3, 1, 1, 1), (2304, 256, 640, 2, 1, 1, 1), (256, 256, 1024, 2, 1, 0, 0),
+                          (300, 96, 640, 1, 0, 1, 0), (100, 200, 130, 1, 1, 1, 0), (130, 32, 4160, 5, 0, 1, 1)])
+def test_gemm_tcgen05_operand_layouts_match_torch(M, N, K, ksplit, a_mn, b_mn, trans_c):
+    """The tcgen05 GEMM with MN-major operands (A given as [K][M], B as
+    [K][N]: the U-Net's weight gradient reads the im2col matrix and dY where
+    they lie) and a transposed C, against torch: 64-wide MN blocks with the
+    128-byte swizzle, a 32-wide B with the 64-byte swizzle, tails in M, N and
+    K, row strides wider than the matrix, split-K."""
+    import torch
+
+    from poisson_caustic_design_gb300 import _lib
+
+    L = _lib.load()
+    g = torch.Generator(device="cpu").manual_seed(M * 3 + N * 5 + K)
+    lda = (M + 7) // 8 * 8 + 8 if a_mn else K + 8
+    ldb = N if b_mn else K
+    As = torch.randn(K if a_mn else M, lda, generator=g).to(torch.bfloat16).cuda()
+    Bs = torch.randn(K if b_mn else N, ldb, generator=g).to(torch.bfloat16).cuda()
+    A = As[:, :M].T if a_mn else As[:, :K]
+    B = Bs[:, :N].T if b_mn else Bs
+    ref = A.float() @ B.float().T
+    ldc = (M + 7) // 8 * 8 + 16 if trans_c else N
+    C = torch.full((N, ldc) if trans_c else (M, ldc), float("nan"), dtype=torch.float32, device="cuda")
+    part = torch.zeros(ksplit * M * N, dtype=torch.float32, device="cuda")
+    st = L.pcd_gemm_bf16_layout(As.data_ptr(), lda, a_mn, Bs.data_ptr(), ldb, b_mn, C.data_ptr(), ldc, trans_c, M, N,
+                                K, ksplit, part.data_ptr(), torch.cuda.current_stream().cuda_stream)
+    assert st == 0, L.pcd_last_error()
+    torch.cuda.synchronize()
+    assert L.pcd_gemm_bf16_status() == 0, L.pcd_last_error()
+    got = C[:, :M].T if trans_c else C[:, :N]
+    err = (got - ref).abs().max().item() / ref.abs().max().item()
+    assert err < 1e-5, err
+    if trans_c:
+        assert torch.isnan(C[:, M:]).all()  # nothing written beyond column M of C[n][:]
+
+
 def torch_unet(params, x, bf16=False):
     """float32 CPU model of the library's U-Net with the flat parameters.
 
@@ -163,6 +201,21 @@ def test_unet_forward_and_gradients_match_torch(ctx):
             rel = np.linalg.norm(go - gt) / nt
             cos = float(go @ gt / (np.linalg.norm(go) * nt + 1e-30))
             assert rel < rel_tol and cos > cos_tol, (name, rel, cos)
+    # the weight gradients through the transposes and the mma.sync kernel
+    # (the GEMM pinned to mma.sync) agree with the MN-major tcgen05 form
+    L = net._L
+    assert L.pcd_gemm_set_default_path(1) == 0
+    try:
+        net.train_step(x, t, lr=0.0)
+        g1 = net.grads()
+    finally:
+        L.pcd_gemm_set_default_path(0)
+    for name, off, shape in layout:
+        if name == "head.b":
+            continue
+        n = g16[name].size
+        rel = np.linalg.norm(g1[off:off + n] - g[off:off + n]) / np.linalg.norm(g[off:off + n])
+        assert rel < 1e-4, (name, rel)
     net.close()
 
 
