@@ -338,6 +338,21 @@ int pcd_gemm_bf16_status(void);
  * form.  No counterpart in the reference. */
 int pcd_gemm_bf16_layout(const void *A, int lda, int a_mn, const void *B, int ldb, int b_mn, float *C, int ldc,
                          int trans_c, int M, int N, int K, int ksplit, float *partials, void *stream);
+/* The U-Net's 3x3, pad-1 convolution as an implicit GEMM on the tcgen05
+ * kernel (no im2col matrix: 4-D TMA boxes of the input, zero-filled outside
+ * the image).  x: BF16 NHWC, B images of H x W, C >= 32 channels (a multiple
+ * of 8) at pixel stride ldx; the images must tile into 128-pixel boxes (64
+ * for the weight gradient), e.g. powers of two.
+ * pcd_conv3x3_bf16: out[p][n] (FP32, row stride ldo) = sum over taps t and
+ * channels c of x[p shifted by t][c] * w[n][t * C + c] (w BF16, row stride
+ * ldw, N output channels).
+ * pcd_conv3x3_wgrad_bf16: dw[n][t * C + c] (FP32, row stride ldw) = sum_p
+ * x[p shifted by t][c] * dy[p][n] (dy BF16 dense [P][N]); ksplit > 1 needs
+ * ksplit * N * 9C floats of partials.  No counterpart in the reference. */
+int pcd_conv3x3_bf16(const void *x, int B, int H, int W, int C, int ldx, const void *w, int ldw, int N, float *out,
+                     int ldo, void *stream);
+int pcd_conv3x3_wgrad_bf16(const void *x, int B, int H, int W, int C, int ldx, const void *dy, int N, float *dw,
+                           int ldw, int ksplit, float *partials, void *stream);
 /* What path 0 (automatic) means for every GEMM of the process, the U-Net's
  * included: 0 (default) tcgen05 wherever it applies (16-byte aligned
  * operands, K >= 64), else mma.sync; 1 mma.sync always. */

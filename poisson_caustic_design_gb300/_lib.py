@@ -172,6 +172,10 @@ SIGNATURES = {
     "pcd_gemm_bf16_path": (C.c_int, [_vp, C.c_int, _vp, C.c_int, _vp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
                                      _vp, C.c_int, _vp]),
     "pcd_gemm_bf16_status": (C.c_int, []),
+    "pcd_conv3x3_bf16": (C.c_int, [_vp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _vp, C.c_int, C.c_int, _vp,
+                                   C.c_int, _vp]),
+    "pcd_conv3x3_wgrad_bf16": (C.c_int, [_vp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _vp, C.c_int, _vp,
+                                         C.c_int, C.c_int, _vp, _vp]),
     "pcd_gemm_bf16_layout": (C.c_int, [_vp, C.c_int, C.c_int, _vp, C.c_int, C.c_int, _vp, C.c_int, C.c_int, C.c_int,
                                        C.c_int, C.c_int, C.c_int, _vp, _vp]),
     "pcd_gemm_set_default_path": (C.c_int, [C.c_int]),

@@ -289,6 +289,34 @@ __global__ void k_relu_bwd(const float *dY, int lddy, const __nv_bfloat16 *Y, in
     }
 }
 
+// The same masking fused with the bias gradient's first pass: block b takes
+// one contiguous range of pixels, thread t channel t % C of every
+// (blockDim / C)-th pixel in it, and part[b][c] = the block's sum of the
+// BF16 values it stored (lanes folded in a fixed order); C divides blockDim.
+__global__ void k_relu_bwd_colsum(const float *dY, int lddy, const __nv_bfloat16 *Y, int ldy, long P, int C, int relu,
+                                  __nv_bfloat16 *dYm, float *part, int chunks)
+{
+    __shared__ float red[256];
+    const int c = threadIdx.x % C, lane = threadIdx.x / C, lanes = blockDim.x / C;
+    const long per = (P + chunks - 1) / chunks;
+    const long p0 = (long)blockIdx.x * per, p1 = min(P, p0 + per);
+    float s = 0.f;
+#pragma unroll 4
+    for (long p = p0 + lane; p < p1; p += lanes) {
+        float d = dY[p * lddy + c];
+        if (relu && !(__bfloat162float(Y[p * ldy + c]) > 0.f)) d = 0.f;
+        const __nv_bfloat16 q = __float2bfloat16(d);
+        dYm[p * C + c] = q;
+        s += __bfloat162float(q);
+    }
+    red[threadIdx.x] = s;
+    __syncthreads();
+    if (lane == 0) {
+        for (int l = 1; l < lanes; l++) s += red[l * C + c];
+        part[(size_t)blockIdx.x * C + c] = s;
+    }
+}
+
 // db[c] = sum_p dYm[p][c]: per-block partials over pixel chunks, fixed order
 __global__ void k_colsum(const __nv_bfloat16 *X, long P, int C, float *part, int chunks)
 {
@@ -301,13 +329,18 @@ __global__ void k_colsum(const __nv_bfloat16 *X, long P, int C, float *part, int
     part[(size_t)blockIdx.y * C + c] = s;
 }
 
-__global__ void k_colsum_fold(const float *part, int chunks, int C, float *out)
+// out[c] = sum_k part[k][c] with one warp per column: lane l adds rows l,
+// l + 32, ... and the lanes fold by shuffles (a fixed order)
+__global__ void k_colsum_fold_warp(const float *part, int chunks, int C, float *out)
 {
-    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    const int c = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
     if (c >= C) return;
     float s = 0.f;
-    for (int k = 0; k < chunks; k++) s += part[(size_t)k * C + c];
-    out[c] = s;
+#pragma unroll 4
+    for (int k = lane; k < chunks; k += 32) s += part[(size_t)k * C + c];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) out[c] = s;
 }
 
 // 2x2 average pool of a channel slice (in stride ldin) into dense out (stride C)
@@ -506,21 +539,86 @@ int set_default_path(int path)
 
 int default_path() { return g_default_path.load(); }
 
+int sm_count()
+{
+    int dev = 0, n = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+        return 1;
+    return n > 0 ? n : 1;
+}
+
+static GemmArgs conv_args(const __nv_bfloat16 *x, int B, int H, int W, int C, int ldx)
+{
+    GemmArgs g{};
+    g.A = x;
+    g.lda = ldx;
+    g.xb = B;
+    g.xh = H;
+    g.xw = W;
+    g.xc = C;
+    g.cwid = C == 32 ? 32 : 64;
+    g.nch = (C + g.cwid - 1) / g.cwid;
+    g.path = 2;
+    return g;
+}
+
+int conv3x3_tc(const __nv_bfloat16 *x, int B, int H, int W, int C, int ldx, const __nv_bfloat16 *w, int ldw, int N,
+               const float *bias, int relu, __nv_bfloat16 *Cb, float *Cf, int ldc, int ksplit, float *partials,
+               cudaStream_t s)
+{
+    GemmArgs g = conv_args(x, B, H, W, C, ldx);
+    g.conv = 1;
+    g.B = w;
+    g.ldb = ldw;
+    g.M = B * H * W;
+    g.N = N;
+    g.K = 9 * C;
+    g.ksplit = ksplit;
+    g.bias = bias;
+    g.relu = relu;
+    g.Cb = Cb;
+    g.Cf = Cf;
+    g.ldc = ldc;
+    return gemm(g, s, ksplit > 1 ? partials : nullptr);
+}
+
+int conv3x3_wgrad_tc(const __nv_bfloat16 *x, int B, int H, int W, int C, int ldx, const __nv_bfloat16 *dy, int N,
+                     float *dw, int ldw, int ksplit, float *partials, cudaStream_t s)
+{
+    GemmArgs g = conv_args(x, B, H, W, C, ldx);
+    g.conv = 2;
+    g.a_mn = 1;
+    g.B = dy;
+    g.ldb = N;
+    g.b_mn = 1;
+    g.trans_c = 1;
+    g.M = 9 * g.nch * g.cwid;
+    g.N = N;
+    g.K = B * H * W;
+    g.ksplit = ksplit;
+    g.Cf = dw;
+    g.ldc = ldw;
+    return gemm(g, s, ksplit > 1 ? partials : nullptr);
+}
+
 size_t gemm_smem(int BN) { return (size_t)GST * (GBM + BN) * SROW * sizeof(__nv_bfloat16); }
 
 int gemm(const GemmArgs &g0, cudaStream_t s, float *partials)
 {
     GemmArgs g = g0;
-    const bool layout_tc = g.a_mn || g.b_mn || g.trans_c;  // forms only the tcgen05 kernel has
+    const bool layout_tc = g.a_mn || g.b_mn || g.trans_c || g.conv;  // forms only the tcgen05 kernel has
     if (layout_tc) {
         if (g.path == 1 || !gemm_tc_applies(g) || g.lda % 8 || g.ldb % 8 || g.M < 1 || g.N < 1 ||
             (g.trans_c && (g.Cb || g.bias || g.relu || !g.Cf))) {
-            set_error("nn gemm: MN-major operands and a transposed C need the tcgen05 path (aligned operands, "
-                      "K >= 64, MN-major extents >= 64, FP32 C without bias or ReLU)");
+            set_error("nn gemm: MN-major operands, implicit convolutions and a transposed C need the tcgen05 path "
+                      "(aligned operands, K >= 64, MN-major extents >= 64, FP32 C without bias or ReLU, images "
+                      "that tile into 128-pixel boxes)");
             return PCD_BAD_ARG;
         }
         g.path = 2;
     }
+    // rows of a transposed C: M, or for the weight gradient 9 taps x channels
+    const int Mo = g.conv == 2 ? 9 * g.xc : g.M;
     if ((!layout_tc && g.K % GBK != 0) || g.lda % 8 || g.ldb % 8 || g.M < 1 || g.N < 1) {
         set_error("nn gemm: K must be a multiple of 32 and leading dimensions multiples of 8");
         return PCD_BAD_ARG;
@@ -538,7 +636,7 @@ int gemm(const GemmArgs &g0, cudaStream_t s, float *partials)
         }
         g.Cf = partials;
         g.Cb = nullptr;
-        g.ldc = g.trans_c ? g.M : g.N;  // partials as [split][M][N], or [split][N][M] for a transposed C
+        g.ldc = g.trans_c ? Mo : g.N;  // partials as [split][M][N], or [split][N][Mo] for a transposed C
     }
     const bool tc = g.path == 2 || (g.path == 0 && g_default_path.load() == 0 && gemm_tc_applies(g) &&
                                     gemm_tc_fills_chip(g));
@@ -564,8 +662,8 @@ int gemm(const GemmArgs &g0, cudaStream_t s, float *partials)
     if (!tc) PCD_LAUNCHED(1);
     if (g.ksplit > 1 && g.trans_c) {
         // the transposed partials reduce as an N x M matrix into C[n][m]
-        k_splitk_reduce<<<grid1d((long)g.M * g.N), 256, 0, s>>>(partials, g.ksplit, g.N, g.M, g.M, nullptr, 0, nullptr,
-                                                               outF, ldo);
+        k_splitk_reduce<<<grid1d((long)Mo * g.N), 256, 0, s>>>(partials, g.ksplit, g.N, Mo, Mo, nullptr, 0, nullptr,
+                                                              outF, ldo);
         PCD_LAUNCHED(1);
     } else if (g.ksplit > 1) {
         k_splitk_reduce<<<grid1d((long)g.M * g.N), 256, 0, s>>>(partials, g.ksplit, g.M, g.N, g.N, g.bias, g.relu,
@@ -610,19 +708,36 @@ int relu_bwd(const float *dY, int lddy, const __nv_bfloat16 *Y, int ldy, long P,
     return PCD_OK;
 }
 
+int relu_bwd_colsum(const float *dY, int lddy, const __nv_bfloat16 *Y, int ldy, long P, int C, int relu,
+                    __nv_bfloat16 *dYm, float *part, long part_cap, float *db, cudaStream_t s)
+{
+    constexpr int kThreads = 256;
+    if (C > kThreads || kThreads % C != 0) {
+        PCD_TRY(relu_bwd(dY, lddy, Y, ldy, P, C, relu, dYm, s));
+        return colsum(dYm, P, C, part, db, s);
+    }
+    // about 128 pixels per block, at most 1024 blocks (and what part holds)
+    const int chunks = (int)std::max<long>(1, std::min<long>(std::min<long>((P + 127) / 128, 1024), part_cap / C));
+    k_relu_bwd_colsum<<<chunks, kThreads, 0, s>>>(dY, lddy, Y, ldy, P, C, relu, dYm, part, chunks);
+    PCD_LAUNCHED(1);
+    k_colsum_fold_warp<<<(C + 7) / 8, 256, 0, s>>>(part, chunks, C, db);
+    PCD_LAUNCHED(1);
+    return PCD_OK;
+}
+
 int colsum(const __nv_bfloat16 *X, long P, int C, float *part, float *out, cudaStream_t s)
 {
     const int chunks = 256;
     k_colsum<<<dim3((C + 63) / 64, chunks), 64, 0, s>>>(X, P, C, part, chunks);
     PCD_LAUNCHED(1);
-    k_colsum_fold<<<(C + 63) / 64, 64, 0, s>>>(part, chunks, C, out);
+    k_colsum_fold_warp<<<(C + 7) / 8, 256, 0, s>>>(part, chunks, C, out);
     PCD_LAUNCHED(1);
     return PCD_OK;
 }
 
 int colsum_f32(const float *part, int rows, int C, float *out, cudaStream_t s)
 {
-    k_colsum_fold<<<(C + 63) / 64, 64, 0, s>>>(part, rows, C, out);
+    k_colsum_fold_warp<<<(C + 7) / 8, 256, 0, s>>>(part, rows, C, out);
     PCD_LAUNCHED(1);
     return PCD_OK;
 }

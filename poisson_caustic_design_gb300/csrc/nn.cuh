@@ -25,6 +25,14 @@ struct GemmArgs {
     // e.g. A given as [K][M] with row stride lda), and C stored transposed
     // (C[n][m] at n * ldc + m; FP32 only, no bias or ReLU)
     int a_mn = 0, b_mn = 0, trans_c = 0;
+    // tcgen05 only: A as the implicit im2col of a 3x3, pad-1 convolution's
+    // input X (NHWC: xb images of xh x xw pixels, xc channels, pixel stride
+    // lda; A points at X).  conv = 1: A[p][k] with k = (tap, chunk of cwid
+    // channels), K tiles tap-major, B the weights [N][9 * xc] (k = tap * xc +
+    // c); conv = 2: the transpose as an MN-major operand for the weight
+    // gradient (M = 9 taps x nch chunks of cwid channels, K = pixels, C stored
+    // transposed at row tap * xc + c).  cwid = 32 for xc = 32, else 64.
+    int conv = 0, xb = 0, xh = 0, xw = 0, xc = 0, cwid = 64, nch = 1;
 };
 
 struct AdamParams {
@@ -54,11 +62,29 @@ int gemm_tc_check(cudaStream_t s);
 // mma.sync; 1 mma.sync always.
 int set_default_path(int path);
 int default_path();
+int sm_count();  // of the current device
+// The 3x3, pad-1 convolution on the tcgen05 kernel without an im2col matrix
+// (4-D TMA boxes of the NHWC input, zero-filled outside the image).
+// conv_tc_applies: whether x (B images of H x W, C >= 32 channels at pixel
+// stride ldx) takes it with T-pixel boxes (T = 128: conv3x3_tc; T = 64:
+// conv3x3_wgrad_tc).  conv3x3_tc: out[p][n] = sum_{tap, c} x[p + tap][c]
+// w[n][tap * C + c] (+ bias, ReLU), BF16 or FP32; conv3x3_wgrad_tc:
+// dw[n][tap * C + c] = sum_p x[p + tap][c] dy[p][n] (dy dense [P][N]).
+bool conv_tc_applies(const void *x, int B, int H, int W, int C, int ldx, int T);
+int conv3x3_tc(const __nv_bfloat16 *x, int B, int H, int W, int C, int ldx, const __nv_bfloat16 *w, int ldw, int N,
+               const float *bias, int relu, __nv_bfloat16 *Cb, float *Cf, int ldc, int ksplit, float *partials,
+               cudaStream_t s);
+int conv3x3_wgrad_tc(const __nv_bfloat16 *x, int B, int H, int W, int C, int ldx, const __nv_bfloat16 *dy, int N,
+                     float *dw, int ldw, int ksplit, float *partials, cudaStream_t s);
 int im2col(const __nv_bfloat16 *in, int B, int H, int W, int C, int ldcin, __nv_bfloat16 *out, int Kp, cudaStream_t s);
 int transpose(const __nv_bfloat16 *in, int rows, int cols, int ldin, __nv_bfloat16 *out, int ldout, cudaStream_t s);
 int flip(const __nv_bfloat16 *Wt, int Cout, int Cin, int Kp, __nv_bfloat16 *Wf, int Kpf, cudaStream_t s);
 int relu_bwd(const float *dY, int lddy, const __nv_bfloat16 *Y, int ldy, long P, int C, int relu, __nv_bfloat16 *dYm,
              cudaStream_t s);
+// relu_bwd and the bias gradient db[c] = sum_p dYm[p][c] in one pass over
+// dY (part: scratch of part_cap floats for the per-block sums)
+int relu_bwd_colsum(const float *dY, int lddy, const __nv_bfloat16 *Y, int ldy, long P, int C, int relu,
+                    __nv_bfloat16 *dYm, float *part, long part_cap, float *db, cudaStream_t s);
 int colsum(const __nv_bfloat16 *X, long P, int C, float *part, float *out, cudaStream_t s);
 // out[c] = sum over rows of part[r][c] (FP32, fixed order)
 int colsum_f32(const float *part, int rows, int C, float *out, cudaStream_t s);

@@ -78,6 +78,16 @@ __device__ __forceinline__ void tma_load_2d(unsigned dst, const CUtensorMap *map
         : "memory");
 }
 
+__device__ __forceinline__ void tma_load_4d(unsigned dst, const CUtensorMap *map, unsigned bar, int c0, int c1, int c2,
+                                            int c3)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4, %5, %6}], "
+        "[%2];" ::"r"(dst),
+        "l"(map), "r"(bar), "r"(c0), "r"(c1), "r"(c2), "r"(c3)
+        : "memory");
+}
+
 // Shared memory descriptor: start address >> 4 (bits 0-13), leading byte
 // offset >> 4 (bits 16-29), stride byte offset >> 4 (bits 32-45), descriptor
 // version 1 (bits 46-47), swizzle mode (bits 61-63: 2 = 128-byte, 4 = 64-byte).
@@ -102,6 +112,12 @@ __device__ __forceinline__ unsigned long long desc_kmajor(unsigned tile, int kk)
     return smem_desc(tile + 32u * kk, 16u, 1024u, 2u);
 }
 
+// K-major with the 64-byte swizzle (32 K values a row): 512-byte atoms
+__device__ __forceinline__ unsigned long long desc_kmajor_sw64(unsigned tile, int kk)
+{
+    return smem_desc(tile + 32u * kk, 16u, 512u, 4u);
+}
+
 __device__ __forceinline__ unsigned long long desc_mnmajor(unsigned tile, int kk, int width)
 {
     return width == 32 ? smem_desc(tile + 1024u * kk, 4096u, 512u, 4u) : smem_desc(tile + 2048u * kk, 8192u, 1024u, 2u);
@@ -116,14 +132,46 @@ __host__ __device__ constexpr unsigned idesc_bf16_f32(int M, int N, int a_mn = 0
            ((unsigned)(N >> 3) << 17) | ((unsigned)(M >> 4) << 24);
 }
 
-// One stage's loads: A (128 rows of M) and B (BN rows of N) for K tile k0.
+// First pixel p0 of a tile -> (image, row, column)
+__device__ __forceinline__ void pixel_of(const GemmArgs &g, int p0, int &b0, int &y0, int &x0)
+{
+    const int hw = g.xh * g.xw;
+    b0 = p0 / hw;
+    const int r = p0 - b0 * hw;
+    y0 = r / g.xw;
+    x0 = r - y0 * g.xw;
+}
+
+// One stage's loads: A (128 rows of M) and B (BN rows of N) for K tile kt.
 // A K-major operand is one box of 64 K columns; an MN-major operand is one
-// box of 64 K rows per 64 (or 32) columns of M / N, 8192 bytes apart.
+// box of 64 K rows per 64 (or 32) columns of M / N, 8192 bytes apart.  An
+// implicit convolution operand is one 4-D box of the input (channels x
+// columns x rows x images) at the tile's pixels shifted by the tap, the
+// coordinates outside the image reading zeros (the convolution's padding):
+// conv = 1, 128 pixels x cwid channels for (tap, chunk) = K tile kt, and the
+// weights' cwid columns of that tap and chunk; conv = 2, for each cwid-wide M
+// block of the tile (one tap and chunk) 64 pixels (K tile kt) x cwid channels.
 template <int BN>
 __device__ __forceinline__ void load_stage(unsigned st, unsigned stB, const CUtensorMap *mA, const CUtensorMap *mB,
-                                           unsigned bar, const GemmArgs &g, int k0, int bm, int bn)
+                                           unsigned bar, const GemmArgs &g, int kt, int bm, int bn)
 {
-    if (g.a_mn) {
+    const int k0 = kt * kTcBK;
+    if (g.conv == 1) {
+        const int t = kt / g.nch, j = kt - t * g.nch;
+        int b0, y0, x0;
+        pixel_of(g, bm, b0, y0, x0);
+        tma_load_4d(st, mA, bar, j * g.cwid, x0 + t % 3 - 1, y0 + t / 3 - 1, b0);
+        tma_load_2d(stB, mB, bar, t * g.xc + j * g.cwid, bn);
+        return;
+    }
+    if (g.conv == 2) {
+        int b0, y0, x0;
+        pixel_of(g, k0, b0, y0, x0);
+        for (int i = 0; i < kTcBM / g.cwid; i++) {
+            const int mb = bm / g.cwid + i, t = mb / g.nch, j = mb - t * g.nch;
+            tma_load_4d(st + (unsigned)(i * 64 * g.cwid * 2), mA, bar, j * g.cwid, x0 + t % 3 - 1, y0 + t / 3 - 1, b0);
+        }
+    } else if (g.a_mn) {
         tma_load_2d(st, mA, bar, bm, k0);
         tma_load_2d(st + 8192u, mA, bar, bm + 64, k0);
     } else {
@@ -153,6 +201,20 @@ __device__ __forceinline__ void mma_commit(unsigned bar)
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
 }
 
+// Row of a transposed C for accumulator row m: m itself, or for the weight
+// gradient (conv = 2) tap * xc + c of the M block's tap and channel; false
+// for rows past M and for the padding channels of a partial chunk.
+__device__ __forceinline__ bool out_row(const GemmArgs &g, int m, int &row)
+{
+    if (g.conv != 2) {
+        row = m;
+        return m < g.M;
+    }
+    const int mb = m / g.cwid, t = mb / g.nch, j = mb - t * g.nch, c = j * g.cwid + (m - mb * g.cwid);
+    row = t * g.xc + c;
+    return m < g.M && t < 9 && c < g.xc;
+}
+
 template <int BN>
 __global__ void __launch_bounds__(kTcThreads, 1)
     k_gemm_tc(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB, GemmArgs g, int *err)
@@ -172,8 +234,10 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     const unsigned ring = (raw + 1023u) & ~1023u;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int bm = blockIdx.y * kTcBM, bn = blockIdx.x * BN;
-    const int KT = (g.K + kTcBK - 1) / kTcBK;
+    const int KT = g.conv == 1 ? 9 * g.nch : (g.K + kTcBK - 1) / kTcBK;
     const int per = (KT + g.ksplit - 1) / g.ksplit;
+    // bytes a stage's loads deliver (a 32-channel convolution tile fills half the stage)
+    const unsigned tx = g.conv == 1 ? (unsigned)(kTcBM + BN) * (unsigned)g.cwid * 2u : kStage;
     const int kt0 = blockIdx.z * per, kt1 = min(KT, kt0 + per);
     const int nk = max(0, kt1 - kt0);
     const unsigned full0 = tc_smem(&bars[0]), empty0 = tc_smem(&bars[kTcStages]), done = tc_smem(&bars[2 * kTcStages]);
@@ -209,8 +273,8 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         const int pre = min(nk, kTcStages);
         for (int i = 0; i < pre; i++) {
             const unsigned st = ring + (unsigned)i * kStage;
-            mbar_expect_tx(full0 + 8 * i, kStage);
-            load_stage<BN>(st, st + kStageA, &mapA, &mapB, full0 + 8 * i, g, (kt0 + i) * kTcBK, bm, bn);
+            mbar_expect_tx(full0 + 8 * i, tx);
+            load_stage<BN>(st, st + kStageA, &mapA, &mapB, full0 + 8 * i, g, kt0 + i, bm, bn);
             s_fills[i]++;
         }
         int issued = pre;
@@ -220,11 +284,19 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             if (!mbar_wait(full0 + 8 * s, phase)) { ok = false; break; }
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
             const unsigned a = ring + (unsigned)s * kStage, b = a + kStageA;
+            const bool k32 = g.conv == 1 && g.cwid == 32;  // a 32-deep K tile (64-byte swizzle)
 #pragma unroll
-            for (int kk = 0; kk < kTcBK / 16; kk++)
-                mma_bf16_tc(tmem, g.a_mn ? desc_mnmajor(a, kk, 64) : desc_kmajor(a, kk),
-                            g.b_mn ? desc_mnmajor(b, kk, BN < 64 ? BN : 64) : desc_kmajor(b, kk), idesc,
-                            (i > 0 || kk > 0) ? 1u : 0u);
+            for (int kk = 0; kk < kTcBK / 16; kk++) {
+                if (k32 && kk >= 2) break;
+                const unsigned long long da = k32         ? desc_kmajor_sw64(a, kk)
+                                              : g.conv == 2 ? desc_mnmajor(a, kk, g.cwid)
+                                              : g.a_mn      ? desc_mnmajor(a, kk, 64)
+                                                            : desc_kmajor(a, kk);
+                const unsigned long long db = k32    ? desc_kmajor_sw64(b, kk)
+                                              : g.b_mn ? desc_mnmajor(b, kk, BN < 64 ? BN : 64)
+                                                       : desc_kmajor(b, kk);
+                mma_bf16_tc(tmem, da, db, idesc, (i > 0 || kk > 0) ? 1u : 0u);
+            }
             mma_commit(empty0 + 8 * s);
             // refill the stage of the previous K tile once its MMAs are done
             if (i > 0 && issued < nk) {
@@ -232,8 +304,8 @@ __global__ void __launch_bounds__(kTcThreads, 1)
                 const unsigned pphase = (unsigned)(((i - 1) / kTcStages) & 1);
                 if (!mbar_wait(empty0 + 8 * ps, pphase)) { ok = false; break; }
                 const unsigned st = ring + (unsigned)ps * kStage;
-                mbar_expect_tx(full0 + 8 * ps, kStage);
-                load_stage<BN>(st, st + kStageA, &mapA, &mapB, full0 + 8 * ps, g, (kt0 + issued) * kTcBK, bm, bn);
+                mbar_expect_tx(full0 + 8 * ps, tx);
+                load_stage<BN>(st, st + kStageA, &mapA, &mapB, full0 + 8 * ps, g, kt0 + issued, bm, bn);
                 s_fills[ps]++;
                 issued++;
             }
@@ -283,8 +355,8 @@ __global__ void __launch_bounds__(kTcThreads, 1)
                     // C[n][m]: a warp's 32 lanes are 32 consecutive m, so each
                     // column n is one 128-byte store (split-K partials as
                     // [split][N][M], ldc = M)
-                    const int m = bm + warp * 32 + lane;
-                    if (m < g.M) {
+                    int m = 0;
+                    if (out_row(g, bm + warp * 32 + lane, m)) {
                         float *base = g.Cf + (g.ksplit > 1 ? (size_t)blockIdx.z * g.N * g.ldc : 0);
 #pragma unroll
                         for (int j = 0; j < 32; j++) {
@@ -319,11 +391,11 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     } else if (nk == 0 && g.ksplit > 1) {
         // an empty K share still writes zero partials
         const int row = bm + warp * 32 + lane;
-        if (row < g.M)
-            for (int n = bn; n < min(g.N, bn + BN); n++) {
-                if (g.trans_c) g.Cf[((size_t)blockIdx.z * g.N + n) * g.ldc + row] = 0.f;
-                else g.Cf[((size_t)blockIdx.z * g.M + row) * g.ldc + n] = 0.f;
-            }
+        int m = 0;
+        if (g.trans_c && out_row(g, row, m))
+            for (int n = bn; n < min(g.N, bn + BN); n++) g.Cf[((size_t)blockIdx.z * g.N + n) * g.ldc + m] = 0.f;
+        else if (!g.trans_c && row < g.M)
+            for (int n = bn; n < min(g.N, bn + BN); n++) g.Cf[((size_t)blockIdx.z * g.M + row) * g.ldc + n] = 0.f;
     }
     if ((s_fail != 0 || lost) && threadIdx.x == 0) {
         // let what is still in flight land before the shared memory and the
@@ -385,6 +457,60 @@ int make_map(CUtensorMap *map, const void *base, int rows, int cols, int ld, int
     return PCD_OK;
 }
 
+// The box of T consecutive pixels of an H x W image batch: (columns, rows,
+// images) = (T, 1, 1) for W a multiple of T, (W, T / W, 1) for W < T with T
+// rows of W dividing H, (W, H, T / (W H)) for whole images; false when the
+// sizes tile no other way (powers of two always do).
+bool conv_box(int W, int H, int T, int box[3])
+{
+    if (W <= 0 || H <= 0) return false;
+    if (W >= T) {
+        if (W % T) return false;
+        box[0] = T, box[1] = 1, box[2] = 1;
+        return true;
+    }
+    if (T % W) return false;
+    const int rows = T / W;
+    if (H >= rows) {
+        if (H % rows) return false;
+        box[0] = W, box[1] = rows, box[2] = 1;
+    } else {
+        if (rows % H) return false;
+        box[0] = W, box[1] = H, box[2] = rows / H;
+    }
+    return true;
+}
+
+// A 4-D tensor map of an NHWC BF16 activation (C channels at pixel stride ldx
+// elements; B images of H x W) with a box of cwid channels x the T-pixel box
+// of conv_box (the 128-byte swizzle for 64 channels, the 64-byte for 32).
+int make_map4(CUtensorMap *map, const void *base, int C, int W, int H, int B, int ldx, int cwid, int T)
+{
+    auto fn = encode_fn();
+    if (!fn) {
+        set_error("tcgen05 conv: cuTensorMapEncodeTiled is not available");
+        return PCD_DEVICE_ERROR;
+    }
+    int bx[3];
+    if (!conv_box(W, H, T, bx)) {
+        set_error("tcgen05 conv: the image size does not tile into boxes of " + std::to_string(T) + " pixels");
+        return PCD_BAD_ARG;
+    }
+    const cuuint64_t dims[4] = {(cuuint64_t)C, (cuuint64_t)W, (cuuint64_t)H, (cuuint64_t)B};
+    const cuuint64_t strides[3] = {(cuuint64_t)ldx * 2, (cuuint64_t)ldx * 2 * W, (cuuint64_t)ldx * 2 * W * H};
+    const cuuint32_t box[4] = {(cuuint32_t)cwid, (cuuint32_t)bx[0], (cuuint32_t)bx[1], (cuuint32_t)bx[2]};
+    const cuuint32_t estr[4] = {1, 1, 1, 1};
+    const CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<void *>(base), dims, strides, box, estr,
+                          CU_TENSOR_MAP_INTERLEAVE_NONE,
+                          cwid == 32 ? CU_TENSOR_MAP_SWIZZLE_64B : CU_TENSOR_MAP_SWIZZLE_128B,
+                          CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) {
+        set_error("tcgen05 conv: cuTensorMapEncodeTiled (4-D) failed (" + std::to_string((int)r) + ")");
+        return PCD_DEVICE_ERROR;
+    }
+    return PCD_OK;
+}
+
 // One error word per device: a kernel that gives up a bounded wait writes a
 // nonzero code there.
 int *err_word()
@@ -434,8 +560,29 @@ int launch_tc(const CUtensorMap &ma, const CUtensorMap &mb, const GemmArgs &g, c
 
 }  // namespace
 
+bool conv_tc_applies(const void *x, int B, int H, int W, int C, int ldx, int T)
+{
+    // every box dimension within the tensor's (a box of more images than the
+    // batch holds is not formed)
+    int box[3];
+    return x && ((uintptr_t)x % 16) == 0 && B >= 1 && C >= 32 && C % 8 == 0 && ldx >= C && ldx % 8 == 0 &&
+           conv_box(W, H, T, box) && box[2] <= B;
+}
+
 bool gemm_tc_applies(const GemmArgs &g)
 {
+    if (g.conv == 1 || g.conv == 2) {
+        const int cw = g.xc == 32 ? 32 : 64;
+        const long P = (long)g.xb * g.xh * g.xw;
+        if (g.cwid != cw || g.nch != (g.xc + cw - 1) / cw || P > (1L << 30) ||
+            !conv_tc_applies(g.A, g.xb, g.xh, g.xw, g.xc, g.lda, g.conv == 1 ? kTcBM : kTcBK))
+            return false;
+        if (g.conv == 1)
+            return g.M == P && g.K == 9 * g.xc && !g.a_mn && !g.b_mn && ((uintptr_t)g.B % 16) == 0 && g.ldb % 8 == 0;
+        return g.M == 9 * g.nch * g.cwid && g.K == P && g.trans_c && g.b_mn && ((uintptr_t)g.B % 16) == 0 &&
+               g.N >= (g.N <= 32 ? 32 : 64);
+    }
+    if (g.conv != 0) return false;
     // TMA: 16-byte aligned bases and row strides (ld multiples of 8, checked
     // by gemm); at least one 64-wide K tile; an MN-major operand at least as
     // wide as its box (64 columns; 32 for a 32-wide B)
@@ -469,10 +616,16 @@ int gemm_tc(const GemmArgs &g, cudaStream_t s)
 {
     CUtensorMap ma, mb;
     const int BN = tc_bn(g.N);
-    if (g.a_mn) PCD_TRY(make_map(&ma, g.A, g.K, g.M, g.lda, kTcBK, 64));
-    else PCD_TRY(make_map(&ma, g.A, g.M, g.K, g.lda, kTcBM));
-    if (g.b_mn) PCD_TRY(make_map(&mb, g.B, g.K, g.N, g.ldb, kTcBK, BN < 64 ? BN : 64));
-    else PCD_TRY(make_map(&mb, g.B, g.N, g.K, g.ldb, BN));
+    if (g.conv == 1) {
+        PCD_TRY(make_map4(&ma, g.A, g.xc, g.xw, g.xh, g.xb, g.lda, g.cwid, kTcBM));
+        PCD_TRY(make_map(&mb, g.B, g.N, g.K, g.ldb, BN, g.cwid));
+    } else {
+        if (g.conv == 2) PCD_TRY(make_map4(&ma, g.A, g.xc, g.xw, g.xh, g.xb, g.lda, g.cwid, kTcBK));
+        else if (g.a_mn) PCD_TRY(make_map(&ma, g.A, g.K, g.M, g.lda, kTcBK, 64));
+        else PCD_TRY(make_map(&ma, g.A, g.M, g.K, g.lda, kTcBM));
+        if (g.b_mn) PCD_TRY(make_map(&mb, g.B, g.K, g.N, g.ldb, kTcBK, BN < 64 ? BN : 64));
+        else PCD_TRY(make_map(&mb, g.B, g.N, g.K, g.ldb, BN));
+    }
     int *err = err_word();
     if (!err) {
         set_error("tcgen05 gemm: no error word");

@@ -126,6 +126,7 @@ struct UNet::Conv {
     __nv_bfloat16 *wb = nullptr;  // [Cout][Kp]
     __nv_bfloat16 *wf = nullptr;  // [Cin][Kpf]
     __nv_bfloat16 *col = nullptr; // [P][Kp]
+    bool col_valid = false;       // col holds the last forward pass's im2col
     const __nv_bfloat16 *in = nullptr;
     int ldin = 0;
     __nv_bfloat16 *out = nullptr;
@@ -229,7 +230,7 @@ int UNet::build(int S_, int maxB_)
     plan.push_back({(void **)&wflip, bf(256 * round32(9 * 384))});
     partials_cap = 32L * 256 * round32(9 * 384);
     plan.push_back({(void **)&partials, f4((long)partials_cap)});
-    plan.push_back({(void **)&colpart, f4(256L * 384)});
+    plan.push_back({(void **)&colpart, f4(kColpartCap)});
     plan.push_back({(void **)&small, f4(512L * 33)});
     plan.push_back({(void **)&lossbuf, f4(4096)});
     plan.push_back({(void **)&xin_f, f4(P0)});
@@ -303,9 +304,25 @@ int UNet::sync_bf16(cudaStream_t s)
     return PCD_OK;
 }
 
+// output tiles of a [P x N] result on the tcgen05 kernel
+static long tc_tiles(long P, int N)
+{
+    const int bn = N <= 32 ? 32 : (N <= 64 ? 64 : (N <= 128 ? 128 : 256));
+    return ((P + 127) / 128) * ((N + bn - 1) / bn);
+}
+
 int UNet::conv_fwd(Conv &c, int B, cudaStream_t s)
 {
+    // an implicit GEMM on the tcgen05 kernel (no im2col matrix) where its
+    // tiles fill the chip; otherwise im2col and the GEMM (split-K for small grids)
+    const long P = (long)B * c.S * c.S;
+    c.col_valid = false;
+    if (nn::default_path() == 0 && c.Kp == 9 * c.Cin && nn::conv_tc_applies(c.in, B, c.S, c.S, c.Cin, c.ldin, 128) &&
+        tc_tiles(P, c.Cout) >= nn::sm_count())
+        return nn::conv3x3_tc(c.in, B, c.S, c.S, c.Cin, c.ldin, c.wb, c.Kp, c.Cout, params_f + c.off_b, c.relu, c.out,
+                              nullptr, c.ldout, 1, nullptr, s);
     PCD_TRY(nn::im2col(c.in, B, c.S, c.S, c.Cin, c.ldin, c.col, c.Kp, s));
+    c.col_valid = true;
     nn::GemmArgs g{};
     g.A = c.col;
     g.lda = c.Kp;
@@ -369,55 +386,75 @@ int UNet::conv_bwd(Conv &c, int B, const float *dY, int lddy, float *dX, cudaStr
 {
     const long P = (long)B * c.S * c.S;
     float *gw = params_f + nparams + c.off_w, *gb = params_f + nparams + c.off_b;
-    PCD_TRY(nn::relu_bwd(dY, lddy, c.out, c.ldout, P, c.Cout, c.relu, dym, s));
-    PCD_TRY(nn::colsum(dym, P, c.Cout, colpart, gb, s));
-    nn::GemmArgs g{};
-    // dW^T[Kp][Cout] = col^T (Kp x P) * dYm (P x Cout) on the tcgen05 kernel,
-    // both operands read where they lie (MN-major: col is [P][Kp], dYm
-    // [P][Cout]) and the result stored transposed into dW[Cout][Kp]; K = P
-    // split so that about two CTAs per SM share it
-    nn::GemmArgs mn{};
-    mn.A = c.col;
-    mn.lda = c.Kp;
-    mn.a_mn = 1;
-    mn.B = dym;
-    mn.ldb = c.Cout;
-    mn.b_mn = 1;
-    mn.M = c.Kp;
-    mn.N = c.Cout;
-    mn.K = (int)P;
-    mn.trans_c = 1;
-    if (nn::default_path() == 0 && nn::gemm_tc_applies(mn)) {
-        g = mn;
-        const int bn = c.Cout <= 32 ? 32 : (c.Cout <= 64 ? 64 : (c.Cout <= 128 ? 128 : 256));
-        const long tiles = (long)((c.Kp + 127) / 128) * ((c.Cout + bn - 1) / bn);
-        int dev = 0, sms = 148;
-        if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    PCD_TRY(nn::relu_bwd_colsum(dY, lddy, c.out, c.ldout, P, c.Cout, c.relu, dym, colpart, kColpartCap, gb, s));
+    const int sms = nn::sm_count();
+    if (nn::default_path() == 0 && c.Kp == 9 * c.Cin && nn::conv_tc_applies(c.in, B, c.S, c.S, c.Cin, c.ldin, 64)) {
+        // dW[Cout][(tap, c)] = sum_p x[p + tap][c] dYm[p][Cout]: the implicit
+        // transposed im2col of the input (MN-major 4-D boxes) against dYm,
+        // K = P split so that about two CTAs per SM share it
+        const int cw = c.Cin == 32 ? 32 : 64;
+        const long Mpad = 9L * ((c.Cin + cw - 1) / cw) * cw;
+        const long tiles = tc_tiles(Mpad, c.Cout);
         const long kt = (P + 63) / 64;
-        g.ksplit = (int)std::max<long>(1, std::min<long>(std::min<long>((2L * sms + tiles - 1) / tiles, kt), 128));
-        while (g.ksplit > 1 && (size_t)g.ksplit * g.M * g.N > partials_cap) g.ksplit /= 2;
+        int ks = (int)std::max<long>(1, std::min<long>(std::min<long>((2L * sms + tiles - 1) / tiles, kt), 128));
+        while (ks > 1 && (size_t)ks * c.Kp * c.Cout > partials_cap) ks /= 2;
+        PCD_TRY(nn::conv3x3_wgrad_tc(c.in, B, c.S, c.S, c.Cin, c.ldin, dym, c.Cout, gw, c.Kp, ks, partials, s));
     } else {
-        // dW[Cout][Kp] = dYm^T (Cout x P) * col (P x Kp): both operands
-        // transposed to K = P contiguous for the mma.sync kernel
-        PCD_TRY(nn::transpose(dym, (int)P, c.Cout, c.Cout, tr_a, (int)P, s));
-        PCD_TRY(nn::transpose(c.col, (int)P, c.Kp, c.Kp, tr_b, (int)P, s));
-        g.A = tr_a;
-        g.lda = (int)P;
-        g.B = tr_b;
-        g.ldb = (int)P;
-        g.M = c.Cout;
-        g.N = c.Kp;
-        g.K = (int)P;
-        const int tiles = ((c.Kp + 127) / 128) * ((c.Cout + 127) / 128);
-        g.ksplit = std::max(1, std::min(32, 1216 / tiles));
+        if (!c.col_valid) {
+            PCD_TRY(nn::im2col(c.in, B, c.S, c.S, c.Cin, c.ldin, c.col, c.Kp, s));
+            c.col_valid = true;
+        }
+        nn::GemmArgs g{};
+        // dW^T[Kp][Cout] = col^T (Kp x P) * dYm (P x Cout) on the tcgen05 kernel,
+        // both operands read where they lie (MN-major: col is [P][Kp], dYm
+        // [P][Cout]) and the result stored transposed into dW[Cout][Kp]; K = P
+        // split so that about two CTAs per SM share it
+        nn::GemmArgs mn{};
+        mn.A = c.col;
+        mn.lda = c.Kp;
+        mn.a_mn = 1;
+        mn.B = dym;
+        mn.ldb = c.Cout;
+        mn.b_mn = 1;
+        mn.M = c.Kp;
+        mn.N = c.Cout;
+        mn.K = (int)P;
+        mn.trans_c = 1;
+        if (nn::default_path() == 0 && nn::gemm_tc_applies(mn)) {
+            g = mn;
+            const int bn = c.Cout <= 32 ? 32 : (c.Cout <= 64 ? 64 : (c.Cout <= 128 ? 128 : 256));
+            const long tiles = (long)((c.Kp + 127) / 128) * ((c.Cout + bn - 1) / bn);
+            const long kt = (P + 63) / 64;
+            g.ksplit = (int)std::max<long>(1, std::min<long>(std::min<long>((2L * sms + tiles - 1) / tiles, kt), 128));
+            while (g.ksplit > 1 && (size_t)g.ksplit * g.M * g.N > partials_cap) g.ksplit /= 2;
+        } else {
+            // dW[Cout][Kp] = dYm^T (Cout x P) * col (P x Kp): both operands
+            // transposed to K = P contiguous for the mma.sync kernel
+            PCD_TRY(nn::transpose(dym, (int)P, c.Cout, c.Cout, tr_a, (int)P, s));
+            PCD_TRY(nn::transpose(c.col, (int)P, c.Kp, c.Kp, tr_b, (int)P, s));
+            g.A = tr_a;
+            g.lda = (int)P;
+            g.B = tr_b;
+            g.ldb = (int)P;
+            g.M = c.Cout;
+            g.N = c.Kp;
+            g.K = (int)P;
+            const int tiles = ((c.Kp + 127) / 128) * ((c.Cout + 127) / 128);
+            g.ksplit = std::max(1, std::min(32, 1216 / tiles));
+        }
+        g.Cf = gw;
+        g.ldc = c.Kp;
+        PCD_TRY(nn::gemm(g, s, partials));
     }
-    g.Cf = gw;
-    g.ldc = c.Kp;
-    PCD_TRY(nn::gemm(g, s, partials));
     if (dX) {
-        // dX = conv(dYm, flipped weights)
-        PCD_TRY(nn::im2col(dym, B, c.S, c.S, c.Cout, c.Cout, colD, c.Kpf, s));
+        // dX = conv(dYm, flipped weights): implicit on the tcgen05 kernel
+        // where its tiles fill the chip, else through im2col
         PCD_TRY(nn::flip(c.wb, c.Cout, c.Cin, c.Kp, wflip, c.Kpf, s));
+        if (nn::default_path() == 0 && c.Kpf == 9 * c.Cout && nn::conv_tc_applies(dym, B, c.S, c.S, c.Cout, c.Cout, 128) &&
+            tc_tiles(P, c.Cin) >= sms)
+            return nn::conv3x3_tc(dym, B, c.S, c.S, c.Cout, c.Cout, wflip, c.Kpf, c.Cin, nullptr, 0, nullptr, dX, c.Cin, 1,
+                                  nullptr, s);
+        PCD_TRY(nn::im2col(dym, B, c.S, c.S, c.Cout, c.Cout, colD, c.Kpf, s));
         nn::GemmArgs d{};
         d.A = colD;
         d.lda = c.Kpf;
@@ -746,6 +783,30 @@ int pcd_gemm_bf16_layout(const void *A, int lda, int a_mn, const void *B, int ld
     g.b_mn = b_mn != 0;
     g.trans_c = trans_c != 0;
     return nn::gemm(g, (cudaStream_t)stream, partials);
+}
+
+int pcd_conv3x3_bf16(const void *x, int B, int H, int W, int C, int ldx, const void *w, int ldw, int N, float *out,
+                     int ldo, void *stream)
+{
+    if (!out || N < 1 || ldo < N || !nn::conv_tc_applies(x, B, H, W, C, ldx, 128)) {
+        set_error("pcd_conv3x3_bf16: unsupported arguments (C >= 32 a multiple of 8, ldx a multiple of 8, aligned x, "
+                  "images tiling into 128-pixel boxes)");
+        return PCD_BAD_ARG;
+    }
+    return nn::conv3x3_tc((const __nv_bfloat16 *)x, B, H, W, C, ldx, (const __nv_bfloat16 *)w, ldw, N, nullptr, 0,
+                          nullptr, out, ldo, 1, nullptr, (cudaStream_t)stream);
+}
+
+int pcd_conv3x3_wgrad_bf16(const void *x, int B, int H, int W, int C, int ldx, const void *dy, int N, float *dw,
+                           int ldw, int ksplit, float *partials, void *stream)
+{
+    if (!dw || N < 32 || ldw < 9 * C || !nn::conv_tc_applies(x, B, H, W, C, ldx, 64)) {
+        set_error("pcd_conv3x3_wgrad_bf16: unsupported arguments (N >= 32, C >= 32 a multiple of 8, aligned x, images "
+                  "tiling into 64-pixel boxes)");
+        return PCD_BAD_ARG;
+    }
+    return nn::conv3x3_wgrad_tc((const __nv_bfloat16 *)x, B, H, W, C, ldx, (const __nv_bfloat16 *)dy, N, dw, ldw,
+                                ksplit, partials, (cudaStream_t)stream);
 }
 
 int pcd_gemm_set_default_path(int path) { return nn::set_default_path(path); }

@@ -20,6 +20,7 @@ struct UNet {
     float *pred, *dpred, *xin_f, *stats;
     // backward scratch
     float *g_a, *g_b, *g_cat, *g_cat2, *g_cat3, *partials, *colpart, *small, *lossbuf;
+    static constexpr long kColpartCap = 1024L * 384;  // floats of colpart (per-block column sums)
     size_t partials_cap = 0;  // floats in partials (split-K of the GEMMs)
     __nv_bfloat16 *dym, *tr_a, *tr_b, *colD, *wflip;
 

@@ -1,0 +1,126 @@
+"""Fixed workloads of the learned warm start's kernels, for timing and for
+profiler captures (each run is deterministic and small enough for a
+full-metric capture of a few launches).
+
+    python -m poisson_caustic_design_gb300.profile_unet gemm [--time]
+        the tcgen05 GEMM on three U-Net contraction shapes (M x N x K):
+        131072 x 32 x 288 (first 32->32 conv at 64^2 x 32), 32768 x 64 x 576
+        (64->64 conv at 32^2 x 32), 16384 x 256 x 2304 (bottom 256->256 conv at
+        32^2 x 16); with --time, CUDA-event medians (L2 flushed between
+        launches) on the tcgen05 and the mma.sync kernels
+    python -m poisson_caustic_design_gb300.profile_unet train R B STEPS [--path P]
+        STEPS training steps of a resolution-R network on batch B (seeded
+        random inputs); with --time, the CUDA-event mean of the steps after the
+        first (--path 1 pins the GEMMs to the mma.sync kernel)
+"""
+import argparse
+import json
+import os
+import sys
+
+SHAPES = ((131072, 32, 288), (32768, 64, 576), (16384, 256, 2304))
+
+
+def _median_ms(fn, reps=20):
+    import torch
+
+    flush = torch.empty(64 << 20, dtype=torch.float32, device="cuda")  # 256 MiB > L2
+    ts = []
+    for _ in range(reps):
+        flush.fill_(1.0)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        fn()
+        e1.record()
+        torch.cuda.synchronize()
+        ts.append(e0.elapsed_time(e1))
+    ts.sort()
+    return ts[len(ts) // 2]
+
+
+def gemm(timed: bool) -> dict:
+    import torch
+
+    from . import _lib
+
+    L = _lib.load()
+    out = {}
+    for M, N, K in SHAPES:
+        g = torch.Generator(device="cpu").manual_seed(M + N + K)
+        A = torch.randn(M, K, generator=g).to(torch.bfloat16).cuda()
+        B = torch.randn(N, K, generator=g).to(torch.bfloat16).cuda()
+        C = torch.empty(M, N, dtype=torch.float32, device="cuda")
+        s = torch.cuda.current_stream().cuda_stream
+        for path in ((2, 1) if timed else (2,)):
+            def run():
+                st = L.pcd_gemm_bf16_path(A.data_ptr(), K, B.data_ptr(), K, C.data_ptr(), N, M, N, K, 1, None, path, s)
+                if st != 0:
+                    raise RuntimeError(L.pcd_last_error())
+
+            run()
+            torch.cuda.synchronize()
+            ref = A.float() @ B.float().T
+            err = (C - ref).abs().max().item() / ref.abs().max().item()
+            if err > 1e-5:
+                raise RuntimeError(f"{M}x{N}x{K} path {path}: relative error {err}")
+            if timed:
+                ms = _median_ms(run)
+                out[f"{M}x{N}x{K}_path{path}"] = {"ms": ms, "tflops": 2.0 * M * N * K / ms / 1e9}
+    if L.pcd_gemm_bf16_status() != 0:
+        raise RuntimeError(L.pcd_last_error())
+    return out
+
+
+def train(R: int, B: int, steps: int, path: int, timed: bool) -> dict:
+    import torch
+
+    from . import Context, learned
+
+    ctx = Context(0)
+    net = learned.UNet(ctx, resolution=R, max_batch=B, seed=1)
+    L = net._L
+    if L.pcd_gemm_set_default_path(path) != 0:
+        raise RuntimeError(L.pcd_last_error())
+    g = torch.Generator(device="cpu").manual_seed(R + B)
+    x = torch.randn(B, R, R, generator=g).cuda()
+    t = torch.randn(B, R, R, generator=g).cuda()
+    loss = net.train_step(x, t, 1e-4)
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(steps - 1):
+        loss = net.train_step(x, t, 1e-4)
+    e1.record()
+    torch.cuda.synchronize()
+    out = {"resolution": R, "batch": B, "loss": loss, "path": path}
+    if timed and steps > 1:
+        out["ms_per_step"] = e0.elapsed_time(e1) / (steps - 1)
+    L.pcd_gemm_set_default_path(0)
+    net.close()
+    return out
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    sub = ap.add_subparsers(dest="what", required=True)
+    a = sub.add_parser("gemm")
+    a.add_argument("--time", action="store_true")
+    b = sub.add_parser("train")
+    b.add_argument("R", type=int)
+    b.add_argument("B", type=int)
+    b.add_argument("steps", type=int)
+    b.add_argument("--path", type=int, default=0)
+    b.add_argument("--time", action="store_true")
+    args = ap.parse_args(argv)
+    if args.what == "gemm":
+        res = gemm(args.time)
+    else:
+        res = train(args.R, args.B, args.steps, args.path, args.time)
+    print(json.dumps(res))
+
+
+if __name__ == "__main__":
+    sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+    main()

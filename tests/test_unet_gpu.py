@@ -104,6 +104,101 @@ def test_gemm_tcgen05_operand_layouts_match_torch(M, N, K, ksplit, a_mn, b_mn, t
         assert torch.isnan(C[:, M:]).all()  # nothing written beyond column M of C[n][:]
 
 
+def _conv_case(B, H, W, C, ldx, off, N, seed):
+    """BF16 NHWC input (C channels at offset off of a buffer with ldx
+    channels a pixel), BF16 weights [N][9C] (k = tap * C + c, tap = 3 dy + dx)
+    and their float CPU copies for torch."""
+    import torch
+
+    g = torch.Generator(device="cpu").manual_seed(seed)
+    buf = torch.randn(B, H, W, ldx, generator=g).to(torch.bfloat16)
+    x = buf[..., off:off + C].float().permute(0, 3, 1, 2).contiguous()  # NCHW
+    w = torch.randn(N, 9 * C, generator=g).to(torch.bfloat16)
+    wt = w.float().reshape(N, 3, 3, C).permute(0, 3, 1, 2).contiguous()  # [N][C][dy][dx]
+    return buf.cuda(), x, w.cuda(), wt
+
+
+@pytest.mark.parametrize("B,H,W,C,ldx,off,N", [(2, 64, 64, 32, 32, 0, 64), (1, 32, 32, 96, 96, 0, 32),
+                                               (4, 8, 8, 256, 256, 0, 128), (1, 16, 256, 64, 192, 128, 256),
+                                               (2, 16, 16, 384, 384, 0, 128), (2, 32, 32, 64, 96, 32, 384)])
+def test_conv3x3_implicit_matches_torch(B, H, W, C, ldx, off, N):
+    """The 3x3 convolution as an implicit GEMM on the tcgen05 kernel (4-D TMA
+    boxes of the NHWC input at each tap's shift, zero-filled outside the image
+    as the padding) against torch.conv2d: 32- and 64-channel chunks, a partial
+    chunk (96 channels), a channel slice of a wider buffer, boxes of whole
+    images (8 x 8 x 2) and of 128-pixel row pieces (width 256), N over 256."""
+    import torch
+    import torch.nn.functional as F
+
+    from poisson_caustic_design_gb300 import _lib
+
+    L = _lib.load()
+    buf, x, w, wt = _conv_case(B, H, W, C, ldx, off, N, B * H * W + C + N)
+    ref = F.conv2d(x, wt, padding=1).permute(0, 2, 3, 1).reshape(B * H * W, N)
+    out = torch.full((B * H * W, N + 8), float("nan"), dtype=torch.float32, device="cuda")
+    st = L.pcd_conv3x3_bf16(buf.data_ptr() + 2 * off, B, H, W, C, ldx, w.data_ptr(), 9 * C, N, out.data_ptr(), N + 8,
+                            torch.cuda.current_stream().cuda_stream)
+    assert st == 0, L.pcd_last_error()
+    torch.cuda.synchronize()
+    assert L.pcd_gemm_bf16_status() == 0, L.pcd_last_error()
+    got = out[:, :N].cpu()
+    err = (got - ref).abs().max().item() / ref.abs().max().item()
+    assert err < 1e-5, err
+    assert torch.isnan(out[:, N:]).all()
+
+
+@pytest.mark.parametrize("B,H,W,C,ldx,off,N,ksplit", [(2, 32, 32, 32, 32, 0, 64, 4), (1, 64, 64, 96, 96, 0, 32, 8),
+                                                      (4, 8, 8, 128, 384, 256, 256, 1), (2, 16, 16, 192, 192, 0, 64, 3),
+                                                      (1, 8, 512, 64, 64, 0, 128, 16)])
+def test_conv3x3_weight_gradient_implicit_matches_torch(B, H, W, C, ldx, off, N, ksplit):
+    """The weight gradient dW[n][tap * C + c] = sum_p x[p + tap][c] dy[p][n]
+    with the transposed implicit im2col as an MN-major operand (one 4-D box of
+    64 pixels per tap and channel chunk) against torch's conv2d_weight:
+    padding channels of a partial chunk dropped, 32-channel chunks, a channel
+    slice, split-K partials reduced."""
+    import torch
+
+    from poisson_caustic_design_gb300 import _lib
+
+    L = _lib.load()
+    buf, x, _, _ = _conv_case(B, H, W, C, ldx, off, N, 7 * B + H + C + N)
+    g = torch.Generator(device="cpu").manual_seed(C + N)
+    dy = torch.randn(B * H * W, N, generator=g).to(torch.bfloat16)
+    dyn = dy.float().reshape(B, H, W, N).permute(0, 3, 1, 2)
+    ref = torch.nn.grad.conv2d_weight(x, (N, C, 3, 3), dyn, padding=1)  # [N][C][dy][dx]
+    ref = ref.permute(0, 2, 3, 1).reshape(N, 9 * C)
+    dw = torch.full((N, 9 * C + 16), float("nan"), dtype=torch.float32, device="cuda")
+    part = torch.zeros(ksplit * N * 9 * C, dtype=torch.float32, device="cuda")
+    dyd = dy.cuda()
+    st = L.pcd_conv3x3_wgrad_bf16(buf.data_ptr() + 2 * off, B, H, W, C, ldx, dyd.data_ptr(), N, dw.data_ptr(),
+                                  9 * C + 16, ksplit, part.data_ptr(), torch.cuda.current_stream().cuda_stream)
+    assert st == 0, L.pcd_last_error()
+    torch.cuda.synchronize()
+    assert L.pcd_gemm_bf16_status() == 0, L.pcd_last_error()
+    got = dw[:, :9 * C].cpu()
+    err = (got - ref).abs().max().item() / ref.abs().max().item()
+    assert err < 1e-5, err
+    assert torch.isnan(dw[:, 9 * C:]).all()
+
+
+def test_conv3x3_implicit_rejects_untileable_sizes():
+    """Image sizes that do not tile into the TMA boxes, channel counts below
+    32 and boxes of more images than the batch are refused (PCD_BAD_ARG), not
+    launched."""
+    import torch
+
+    from poisson_caustic_design_gb300 import _lib
+
+    L = _lib.load()
+    x = torch.zeros(2 * 24 * 24 * 64, dtype=torch.bfloat16, device="cuda")
+    w = torch.zeros(32 * 9 * 64, dtype=torch.bfloat16, device="cuda")
+    out = torch.zeros(2 * 24 * 24 * 64, dtype=torch.float32, device="cuda")
+    s = torch.cuda.current_stream().cuda_stream
+    assert L.pcd_conv3x3_bf16(x.data_ptr(), 2, 24, 24, 64, 64, w.data_ptr(), 576, 32, out.data_ptr(), 32, s) == 2
+    assert L.pcd_conv3x3_bf16(x.data_ptr(), 2, 16, 16, 16, 16, w.data_ptr(), 144, 32, out.data_ptr(), 32, s) == 2
+    assert L.pcd_conv3x3_bf16(x.data_ptr(), 1, 8, 8, 64, 64, w.data_ptr(), 576, 32, out.data_ptr(), 32, s) == 2
+
+
 def torch_unet(params, x, bf16=False):
     """float32 CPU model of the library's U-Net with the flat parameters.
 
