@@ -322,8 +322,11 @@ int pcd_gemm_bf16(const void *A, int lda, const void *B, int ldb, float *C, int 
                   int ksplit, float *partials, void *stream);
 /* The same GEMM on a chosen path: 0 automatic, 1 mma.sync (warp-level
  * tensor-core fragments through ldmatrix), 2 tcgen05 (TMA loads with the
- * 128-byte swizzle, tcgen05.mma into a tensor-memory accumulator; A and B
- * 16-byte aligned).  The tcgen05 kernel's bounded waits report through a
+ * 128-byte swizzle, tcgen05.mma into tensor-memory accumulators; one
+ * or two persistent CTAs per SM with a TMA warp, an MMA warp and four
+ * epilogue warps, two accumulators so that a tile's epilogue overlaps the
+ * next tile; A and B 16-byte aligned).  The tcgen05 kernel's bounded waits
+ * report through a
  * device error word that pcd_gemm_bf16_status reads (after synchronising the
  * device; PCD_TIMEOUT if a wait gave up since the last call) and clears.  No
  * counterpart in the reference. */

@@ -20,7 +20,7 @@ struct GemmArgs {
     __nv_bfloat16 *Cb;       // BF16 output (row stride ldc), or
     float *Cf;               // FP32 output
     int ldc;
-    int path = 0;            // 0 automatic, 1 mma.sync, 2 tcgen05 (TMA + tensor memory)
+    int path = 0;            // 0 automatic, 1 mma.sync, 2 tcgen05 (persistent, warp-specialised)
     // tcgen05 only: an operand stored K-rows x M (or N) contiguous ("MN-major",
     // e.g. A given as [K][M] with row stride lda), and C stored transposed
     // (C[n][m] at n * ldc + m; FP32 only, no bias or ReLU)

@@ -1,29 +1,28 @@
 // nn_tc.cu -- the U-Net's BF16 GEMM on the 5th-generation tensor cores
 // (tcgen05, sm_103a).
 //
-// C[M x N] = A[M x K] * B[N x K]^T with A and B BF16 row-major, K contiguous
-// ("TN", the layout of nn::gemm), FP32 accumulation in tensor memory.  One CTA
-// computes a 128 x BN tile of C over its share of K:
-//
-//   * TMA (cp.async.bulk.tensor.2d) loads 128 x 64 tiles of A and BN x 64
-//     tiles of B into shared memory with the 128-byte swizzle, through a ring
-//     of kStages stages (full / empty mbarriers; the transfer size is the
-//     whole box, zero-filled where the box leaves the matrix);
-//   * one thread issues tcgen05.mma.cta_group::1.kind::f16 (M = 128, N = BN,
-//     K = 16 per instruction, both operands K-major, described by shared
-//     memory descriptors whose start address steps 32 bytes per K slice
-//     inside the 128-byte swizzle atom) into a 128-lane x BN-column FP32
-//     accumulator in tensor memory, and tcgen05.commit signals the stage free
-//     once the MMAs that read it are done;
-//   * after the last MMA, warps 0-3 read their 32 lanes (rows) of the
-//     accumulator with tcgen05.ld.32x32b and apply the epilogue of nn::gemm
-//     (bias, ReLU, BF16 or FP32 store, or FP32 split-K partials).
-//
-// The same thread produces and consumes the ring: it refills the stage the
-// previous K tile used once that tile's MMAs have completed, while the MMAs
-// of the current tile run.  Every mbarrier wait is bounded: a wait that runs
-// out records PCD_TIMEOUT in *err, the CTA stops issuing, waits (bounded) for
-// what it has in flight and frees its tensor memory.
+// C[M x N] = A[M x K] * B[N x K]^T, FP32 accumulation in tensor memory.  The
+// operands come in by TMA (cp.async.bulk.tensor) with the 128-byte swizzle
+// (64-byte for 32-wide tiles), as
+//   * K-major 2-D tiles (A, B row-major with K contiguous: "TN", the layout of
+//     nn::gemm),
+//   * MN-major 2-D tiles (an operand stored K rows x M or N contiguous: the
+//     weight gradient reads the activations and dY where they lie),
+//   * implicit 3x3 convolution tiles: 4-D boxes (channels x columns x rows x
+//     images) of the NHWC input at each tap's shift, the coordinates outside
+//     the image zero-filled by TMA, which is the convolution's padding -- the
+//     im2col matrix is never formed (forward and data gradient as K-major A,
+//     weight gradient as MN-major A);
+// and one elected thread issues tcgen05.mma.cta_group::1.kind::f16 (M = 128,
+// N = BN, K = 16 per instruction) on shared memory descriptors.  The kernel
+// (k_gemm_tcp, described above it) is persistent and warp-specialised: a TMA
+// warp, an MMA warp and four epilogue warps, two accumulators in tensor
+// memory so that a tile's epilogue overlaps the next tile's loads and MMAs.
+// The epilogue reads the accumulator with tcgen05.ld.32x32b and applies
+// nn::gemm's (bias, ReLU, BF16 or FP32 store, FP32 split-K partials, or a
+// transposed store).  Every mbarrier wait is bounded: a wait that runs out
+// records PCD_TIMEOUT in an error word, the CTA stops issuing, waits
+// (bounded) for what it has in flight and frees its tensor memory.
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <cudaTypedefs.h>
@@ -37,7 +36,7 @@ namespace nn {
 
 namespace {
 
-constexpr int kTcBM = 128, kTcBK = 64, kTcStages = 4, kTcThreads = 128;
+constexpr int kTcBM = 128, kTcBK = 64;
 constexpr long long kTcSpin = 1ll << 24;
 
 __device__ __forceinline__ unsigned tc_smem(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
@@ -215,47 +214,107 @@ __device__ __forceinline__ bool out_row(const GemmArgs &g, int m, int &row)
     return m < g.M && t < 9 && c < g.xc;
 }
 
+// ---------------------------------------------------------------------------
+// The persistent form: one CTA per SM (two for N tiles up to 64) walks the
+// output tiles (units of 128 x BN x one K share, M fastest so that CTAs
+// running together share B), with three roles so that nothing waits for a
+// tile's end:
+//   warp 0 (one lane): TMA producer over a ring of nst stages, running ahead
+//     across unit boundaries (waits: the stage's empty barrier);
+//   warp 1 (one lane): MMA issuer into one of two tensor-memory accumulators
+//     (2 x BN columns), alternating per unit; commits free each stage and,
+//     after a unit's last K tile, signal its accumulator full (waits: the
+//     stage's full barrier, the accumulator's empty barrier);
+//   warps 2-5: epilogue; warp w reads accumulator lanes 32 (w % 4) + [0, 32)
+//     (the quarter its warp slot may access), stores the rows (or, for a
+//     transposed C, the columns) and releases the accumulator (one arrive
+//     per warp; the barrier counts 4).
+// The epilogue of one unit overlaps the loads and MMAs of the next.  Every
+// wait is bounded: the first to run out records PCD_TIMEOUT and raises a
+// shared abort flag that the other roles' loops test; before freeing tensor
+// memory the CTA waits (bounded) for its MMAs and its last loads.
+constexpr int kTpThreads = 192, kTpMaxStages = 12;
+constexpr unsigned kTpStageBytes = 4u * 32u * 33u * 4u;  // epilogue: a [32][33] float tile per warp
+
+// CTAs per SM: two for N tiles up to 64 (their units are short; two CTAs
+// hide each other's unit boundaries), else one; and the stage ring's share
+// of shared memory (227 KB per SM less the epilogue tiles and slack).
+__host__ __device__ constexpr int tp_ctas_per_sm(int BN) { return BN <= 64 ? 2 : 1; }
+__host__ __device__ constexpr unsigned tp_ring_budget(int BN)
+{
+    return (227u * 1024u) / (unsigned)tp_ctas_per_sm(BN) - kTpStageBytes - 2048u;
+}
+
+__host__ __device__ inline unsigned tp_stage_a(const GemmArgs &g)
+{
+    return (g.conv == 1 && g.cwid == 32) ? kTcBM * 32 * 2 : kTcBM * kTcBK * 2;
+}
+
+__host__ __device__ inline unsigned tp_stage_b(const GemmArgs &g, int BN)
+{
+    return (unsigned)BN * ((g.conv == 1 && g.cwid == 32) ? 32u : (unsigned)kTcBK) * 2u;
+}
+
+__host__ __device__ inline unsigned tp_stride(const GemmArgs &g, int BN)
+{
+    return (tp_stage_a(g) + tp_stage_b(g, BN) + 1023u) & ~1023u;
+}
+
+__device__ __forceinline__ void mbar_arrive(unsigned bar)
+{
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+
 template <int BN>
-__global__ void __launch_bounds__(kTcThreads, 1)
-    k_gemm_tc(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB, GemmArgs g, int *err)
+__global__ void __launch_bounds__(kTpThreads, tp_ctas_per_sm(BN))
+    k_gemm_tcp(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB, GemmArgs g, int nst,
+               int *err)
 {
     static_assert(BN == 32 || BN == 64 || BN == 128 || BN == 256, "N tile");
-    static_assert(kTcBM * 33 * 4 <= kTcStages * (kTcBM * kTcBK * 2), "epilogue tile fits in the ring");
-    constexpr unsigned kStageA = kTcBM * kTcBK * 2, kStageB = BN * kTcBK * 2, kStage = kStageA + kStageB;
-    constexpr int kCols = BN < 32 ? 32 : BN;  // tensor memory columns (a power of 2, >= 32)
+    constexpr int kCols = 2 * BN;  // two accumulators (a power of 2, >= 64)
     extern __shared__ __align__(1024) unsigned char tc_buf[];
-    __shared__ __align__(8) unsigned long long bars[2 * kTcStages + 1];
+    __shared__ __align__(8) unsigned long long bars[2 * kTpMaxStages + 5];
     __shared__ unsigned tmem_base;
-    __shared__ int s_fail;
-    __shared__ int s_fills[kTcStages];  // loads issued per stage (thread 0)
+    __shared__ volatile int s_abort;
+    __shared__ int s_fills[kTpMaxStages];  // loads issued per stage (producer)
 
-    // the ring must start on a 1024-byte boundary (the swizzle atom)
     const unsigned raw = tc_smem(tc_buf);
     const unsigned ring = (raw + 1023u) & ~1023u;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int bm = blockIdx.y * kTcBM, bn = blockIdx.x * BN;
+    const bool k32 = g.conv == 1 && g.cwid == 32;
+    const unsigned aBytes = tp_stage_a(g), tx = aBytes + tp_stage_b(g, BN), sstride = tp_stride(g, BN);
+    const int MT = (g.M + kTcBM - 1) / kTcBM, NT = (g.N + BN - 1) / BN;
+    const int units = MT * NT * g.ksplit;
     const int KT = g.conv == 1 ? 9 * g.nch : (g.K + kTcBK - 1) / kTcBK;
     const int per = (KT + g.ksplit - 1) / g.ksplit;
-    // bytes a stage's loads deliver (a 32-channel convolution tile fills half the stage)
-    const unsigned tx = g.conv == 1 ? (unsigned)(kTcBM + BN) * (unsigned)g.cwid * 2u : kStage;
-    const int kt0 = blockIdx.z * per, kt1 = min(KT, kt0 + per);
-    const int nk = max(0, kt1 - kt0);
-    const unsigned full0 = tc_smem(&bars[0]), empty0 = tc_smem(&bars[kTcStages]), done = tc_smem(&bars[2 * kTcStages]);
+    const unsigned bar0 = tc_smem(&bars[0]);
+    auto full = [&](int s) { return bar0 + 8u * s; };
+    auto empty = [&](int s) { return bar0 + 8u * (kTpMaxStages + s); };
+    auto tfull = [&](int a) { return bar0 + 8u * (2 * kTpMaxStages + a); };
+    auto tempty = [&](int a) { return bar0 + 8u * (2 * kTpMaxStages + 2 + a); };
+    const unsigned drain = bar0 + 8u * (2 * kTpMaxStages + 4);
+    auto fail = [&]() {
+        atomicCAS(err, 0, PCD_TIMEOUT);
+        s_abort = 1;
+    };
 
     if (threadIdx.x == 0) {
-        s_fail = 0;
-        for (int s = 0; s < kTcStages; s++) {
+        s_abort = 0;
+        for (int s = 0; s < nst; s++) {
             s_fills[s] = 0;
-            mbar_init(full0 + 8 * s, 1);
-            mbar_init(empty0 + 8 * s, 1);
+            mbar_init(full(s), 1);
+            mbar_init(empty(s), 1);
         }
-        mbar_init(done, 1);
+        for (int a = 0; a < 2; a++) {
+            mbar_init(tfull(a), 1);
+            mbar_init(tempty(a), 4);
+        }
+        mbar_init(drain, 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         asm volatile("prefetch.tensormap [%0];" ::"l"(&mapA) : "memory");
         asm volatile("prefetch.tensormap [%0];" ::"l"(&mapB) : "memory");
     }
     if (warp == 0) {
-        // one warp allocates the accumulator's columns (and frees them at the end)
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(tc_smem(&tmem_base)),
                      "r"(kCols)
                      : "memory");
@@ -266,145 +325,158 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const unsigned tmem = tmem_base;
 
-    // ---- producer + MMA issuer: thread 0
-    if (threadIdx.x == 0 && nk > 0) {
-        const unsigned idesc = idesc_bf16_f32(kTcBM, BN, g.a_mn, g.b_mn);
-        bool ok = true;
-        const int pre = min(nk, kTcStages);
-        for (int i = 0; i < pre; i++) {
-            const unsigned st = ring + (unsigned)i * kStage;
-            mbar_expect_tx(full0 + 8 * i, tx);
-            load_stage<BN>(st, st + kStageA, &mapA, &mapB, full0 + 8 * i, g, kt0 + i, bm, bn);
-            s_fills[i]++;
+    if (warp == 0) {
+        if (lane == 0) {
+            int it = 0;
+            for (int u = blockIdx.x; u < units && !s_abort; u += gridDim.x) {
+                const int mt = u % MT, r = u / MT, nt = r % NT, z = r / NT;
+                const int k0 = z * per, nk = max(0, min(KT, k0 + per) - k0);
+                for (int i = 0; i < nk; i++, it++) {
+                    const int s = it % nst, round = it / nst;
+                    if (round > 0 && !mbar_wait(empty(s), (unsigned)((round - 1) & 1))) {
+                        fail();
+                        break;
+                    }
+                    if (s_abort) break;
+                    const unsigned st = ring + (unsigned)s * sstride;
+                    mbar_expect_tx(full(s), tx);
+                    load_stage<BN>(st, st + aBytes, &mapA, &mapB, full(s), g, k0 + i, mt * kTcBM, nt * BN);
+                    s_fills[s]++;
+                }
+            }
         }
-        int issued = pre;
-        for (int i = 0; i < nk && ok; i++) {
-            const int s = i % kTcStages;
-            const unsigned phase = (unsigned)((i / kTcStages) & 1);
-            if (!mbar_wait(full0 + 8 * s, phase)) { ok = false; break; }
-            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            const unsigned a = ring + (unsigned)s * kStage, b = a + kStageA;
-            const bool k32 = g.conv == 1 && g.cwid == 32;  // a 32-deep K tile (64-byte swizzle)
+    } else if (warp == 1) {
+        if (lane == 0) {
+            const unsigned idesc = idesc_bf16_f32(kTcBM, BN, g.a_mn, g.b_mn);
+            int it = 0, lu = 0;
+            for (int u = blockIdx.x; u < units && !s_abort; u += gridDim.x, lu++) {
+                const int r = u / MT, z = r / NT;
+                const int k0 = z * per, nk = max(0, min(KT, k0 + per) - k0);
+                const int a = lu & 1, use = lu >> 1;
+                if (use > 0 && !mbar_wait(tempty(a), (unsigned)((use - 1) & 1))) {
+                    fail();
+                    break;
+                }
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                const unsigned acc = tmem + (unsigned)(a * BN);
+                for (int i = 0; i < nk && !s_abort; i++, it++) {
+                    const int s = it % nst, round = it / nst;
+                    if (!mbar_wait(full(s), (unsigned)(round & 1))) {
+                        fail();
+                        break;
+                    }
+                    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                    const unsigned sa = ring + (unsigned)s * sstride, sb = sa + aBytes;
 #pragma unroll
-            for (int kk = 0; kk < kTcBK / 16; kk++) {
-                if (k32 && kk >= 2) break;
-                const unsigned long long da = k32         ? desc_kmajor_sw64(a, kk)
-                                              : g.conv == 2 ? desc_mnmajor(a, kk, g.cwid)
-                                              : g.a_mn      ? desc_mnmajor(a, kk, 64)
-                                                            : desc_kmajor(a, kk);
-                const unsigned long long db = k32    ? desc_kmajor_sw64(b, kk)
-                                              : g.b_mn ? desc_mnmajor(b, kk, BN < 64 ? BN : 64)
-                                                       : desc_kmajor(b, kk);
-                mma_bf16_tc(tmem, da, db, idesc, (i > 0 || kk > 0) ? 1u : 0u);
-            }
-            mma_commit(empty0 + 8 * s);
-            // refill the stage of the previous K tile once its MMAs are done
-            if (i > 0 && issued < nk) {
-                const int ps = (i - 1) % kTcStages;
-                const unsigned pphase = (unsigned)(((i - 1) / kTcStages) & 1);
-                if (!mbar_wait(empty0 + 8 * ps, pphase)) { ok = false; break; }
-                const unsigned st = ring + (unsigned)ps * kStage;
-                mbar_expect_tx(full0 + 8 * ps, tx);
-                load_stage<BN>(st, st + kStageA, &mapA, &mapB, full0 + 8 * ps, g, kt0 + issued, bm, bn);
-                s_fills[ps]++;
-                issued++;
+                    for (int kk = 0; kk < kTcBK / 16; kk++) {
+                        if (k32 && kk >= 2) break;
+                        const unsigned long long da = k32         ? desc_kmajor_sw64(sa, kk)
+                                                      : g.conv == 2 ? desc_mnmajor(sa, kk, g.cwid)
+                                                      : g.a_mn      ? desc_mnmajor(sa, kk, 64)
+                                                                    : desc_kmajor(sa, kk);
+                        const unsigned long long db = k32    ? desc_kmajor_sw64(sb, kk)
+                                                      : g.b_mn ? desc_mnmajor(sb, kk, BN < 64 ? BN : 64)
+                                                               : desc_kmajor(sb, kk);
+                        mma_bf16_tc(acc, da, db, idesc, (i > 0 || kk > 0) ? 1u : 0u);
+                    }
+                    mma_commit(empty(s));
+                }
+                if (s_abort) break;
+                mma_commit(tfull(a));  // arrives once this unit's MMAs are done (at once when it had none)
             }
         }
-        if (ok) {
-            mma_commit(done);  // arrives when every MMA issued above has completed
-        } else {
-            atomicCAS(err, 0, PCD_TIMEOUT);
-            s_fail = 1;
-        }
-    }
-    __syncthreads();
-
-    // ---- epilogue: 32 columns at a time, warp w reading accumulator lanes
-    // [32w, 32w + 32) (tile rows) with tcgen05.ld, through a shared tile in
-    // the (now idle) ring so that the stores of C run along its rows
-    const bool fail = s_fail != 0 || nk == 0;  // the same for every thread (read after a barrier)
-    bool lost = false;                         // the done wait ran out somewhere in the block
-    if (!fail) {
-        // one decision for the whole block: every thread takes the same path
-        // through the barriers below
-        const bool ok = __syncthreads_and(mbar_wait(done, 0u)) != 0;
-        lost = !ok;
-        if (!ok && threadIdx.x == 0) atomicCAS(err, 0, PCD_TIMEOUT);
-        if (ok) {
+    } else {
+        const int q = warp & 3;  // the accumulator lane quarter this warp may read
+        float *tile = reinterpret_cast<float *>(tc_buf + (ring - raw) + (size_t)nst * sstride) + (warp - 2) * 32 * 33;
+        int lu = 0;
+        for (int u = blockIdx.x; u < units; u += gridDim.x, lu++) {
+            const int mt = u % MT, r = u / MT, nt = r % NT, z = r / NT;
+            const int k0 = z * per, nk = max(0, min(KT, k0 + per) - k0);
+            const int a = lu & 1, use = lu >> 1;
+            const bool ok = __all_sync(0xffffffffu, s_abort == 0 && mbar_wait(tfull(a), (unsigned)(use & 1)));
+            if (!ok) {
+                if (lane == 0) fail();
+                break;
+            }
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            float *tile = reinterpret_cast<float *>(tc_buf + (ring - raw));  // [128][33]
+            const int m = mt * kTcBM + q * 32 + lane;
             for (int c0 = 0; c0 < BN; c0 += 32) {
-                unsigned r[32];
-                const unsigned addr = tmem + ((unsigned)(warp * 32) << 16) + (unsigned)c0;
-                asm volatile(
-                    "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
-                    "[%16];"
-                    : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-                      "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
-                      "=r"(r[15])
-                    : "r"(addr));
-                asm volatile(
-                    "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
-                    "[%16];"
-                    : "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]),
-                      "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]),
-                      "=r"(r[30]), "=r"(r[31])
-                    : "r"(addr + 16u));
-                asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-                if (g.trans_c) {
-                    // C[n][m]: a warp's 32 lanes are 32 consecutive m, so each
-                    // column n is one 128-byte store (split-K partials as
-                    // [split][N][M], ldc = M)
-                    int m = 0;
-                    if (out_row(g, bm + warp * 32 + lane, m)) {
-                        float *base = g.Cf + (g.ksplit > 1 ? (size_t)blockIdx.z * g.N * g.ldc : 0);
+                unsigned v[32];
+                if (nk > 0) {
+                    const unsigned addr = tmem + ((unsigned)(q * 32) << 16) + (unsigned)(a * BN + c0);
+                    asm volatile(
+                        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,"
+                        "%15}, [%16];"
+                        : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
+                          "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]),
+                          "=r"(v[14]), "=r"(v[15])
+                        : "r"(addr));
+                    asm volatile(
+                        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,"
+                        "%15}, [%16];"
+                        : "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]),
+                          "=r"(v[23]), "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]),
+                          "=r"(v[30]), "=r"(v[31])
+                        : "r"(addr + 16u));
+                    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+                } else {
 #pragma unroll
-                        for (int j = 0; j < 32; j++) {
-                            const int n = bn + c0 + j;
-                            if (n < g.N) base[(size_t)n * g.ldc + m] = __uint_as_float(r[j]);
-                        }
+                    for (int j = 0; j < 32; j++) v[j] = 0u;  // an empty K share: zero partials
+                }
+                const int n0 = nt * BN + c0;
+                if (g.trans_c) {
+                    int row = 0;
+                    if (out_row(g, m, row)) {
+                        float *base = g.Cf + (g.ksplit > 1 ? (size_t)z * g.N * g.ldc : 0);
+#pragma unroll
+                        for (int j = 0; j < 32; j++)
+                            if (n0 + j < g.N) base[(size_t)(n0 + j) * g.ldc + row] = __uint_as_float(v[j]);
                     }
                     continue;
                 }
-                float *mine = tile + (warp * 32 + lane) * 33;
+                // through the warp's shared tile: lane l then stores column
+                // n0 + l of the warp's 32 rows, a row per instruction
 #pragma unroll
-                for (int j = 0; j < 32; j++) mine[j] = __uint_as_float(r[j]);
-                __syncthreads();
-                const int n = bn + c0 + lane;
-                const float bias = (g.ksplit == 1 && g.bias && n < g.N) ? g.bias[n] : 0.f;
-                for (int rr = warp; rr < kTcBM; rr += kTcThreads / 32) {
-                    const int row = bm + rr;
-                    if (row >= g.M || n >= g.N) continue;
-                    float v = tile[rr * 33 + lane];
-                    if (g.ksplit > 1) {
-                        g.Cf[((size_t)blockIdx.z * g.M + row) * g.ldc + n] = v;
-                        continue;
+                for (int jj = 0; jj < 32; jj++) tile[lane * 33 + jj] = __uint_as_float(v[jj]);
+                __syncwarp();
+                const int n = n0 + lane;
+                if (n < g.N) {
+                    const float bias = (g.ksplit == 1 && g.bias) ? g.bias[n] : 0.f;
+                    for (int rr = 0; rr < 32; rr++) {
+                        const int row = mt * kTcBM + q * 32 + rr;
+                        if (row >= g.M) break;
+                        float x = tile[rr * 33 + lane];
+                        if (g.ksplit > 1) {
+                            g.Cf[((size_t)z * g.M + row) * g.ldc + n] = x;
+                            continue;
+                        }
+                        x += bias;
+                        if (g.relu) x = fmaxf(x, 0.f);
+                        if (g.Cb) g.Cb[(size_t)row * g.ldc + n] = __float2bfloat16(x);
+                        else g.Cf[(size_t)row * g.ldc + n] = x;
                     }
-                    v += bias;
-                    if (g.relu) v = fmaxf(v, 0.f);
-                    if (g.Cb) g.Cb[(size_t)row * g.ldc + n] = __float2bfloat16(v);
-                    else g.Cf[(size_t)row * g.ldc + n] = v;
                 }
-                __syncthreads();
+                __syncwarp();
             }
+            // release the accumulator: every lane's loads have completed
+            asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+            __syncwarp();
+            if (lane == 0) mbar_arrive(tempty(a));
         }
-    } else if (nk == 0 && g.ksplit > 1) {
-        // an empty K share still writes zero partials
-        const int row = bm + warp * 32 + lane;
-        int m = 0;
-        if (g.trans_c && out_row(g, row, m))
-            for (int n = bn; n < min(g.N, bn + BN); n++) g.Cf[((size_t)blockIdx.z * g.N + n) * g.ldc + m] = 0.f;
-        else if (!g.trans_c && row < g.M)
-            for (int n = bn; n < min(g.N, bn + BN); n++) g.Cf[((size_t)blockIdx.z * g.M + row) * g.ldc + n] = 0.f;
     }
-    if ((s_fail != 0 || lost) && threadIdx.x == 0) {
-        // let what is still in flight land before the shared memory and the
-        // tensor memory go away: every MMA issued (one more commit), and each
-        // stage's latest load (bounded waits)
-        mma_commit(done);
-        (void)mbar_wait(done, 0u);
-        for (int s = 0; s < kTcStages; s++)
-            if (s_fills[s] > 0) (void)mbar_wait(full0 + 8 * s, (unsigned)((s_fills[s] - 1) & 1));
+
+    __syncthreads();
+    if (s_abort) {
+        // let what is in flight land before the tensor memory and the shared
+        // memory go away: every MMA issued (a last commit), every stage's
+        // latest load (bounded waits)
+        if (warp == 1 && lane == 0) {
+            mma_commit(drain);
+            (void)mbar_wait(drain, 0u);
+        }
+        if (warp == 0 && lane == 0)
+            for (int s = 0; s < nst; s++)
+                if (s_fills[s] > 0) (void)mbar_wait(full(s), (unsigned)((s_fills[s] - 1) & 1));
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
@@ -526,15 +598,7 @@ int *err_word()
 }
 
 template <int BN>
-constexpr size_t tc_smem_bytes()
-{
-    return (size_t)kTcStages * (kTcBM * kTcBK * 2 + BN * kTcBK * 2) + 1024;
-}
-
-// The kernel's shared-memory attribute, set on the current device the first
-// time (the setting belongs to the function on that device).
-template <int BN>
-int tc_attr()
+int tcp_attr()
 {
     static std::mutex mu;
     static unsigned long long done_mask = 0;
@@ -542,18 +606,22 @@ int tc_attr()
     PCD_CUDA(cudaGetDevice(&dev));
     std::lock_guard<std::mutex> lk(mu);
     if (dev < 64 && (done_mask >> dev & 1ull)) return PCD_OK;
-    PCD_CUDA(cudaFuncSetAttribute(k_gemm_tc<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tc_smem_bytes<BN>()));
+    PCD_CUDA(cudaFuncSetAttribute(k_gemm_tcp<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)(tp_ring_budget(BN) + kTpStageBytes + 1024u)));
     if (dev < 64) done_mask |= 1ull << dev;
     return PCD_OK;
 }
 
 template <int BN>
-int launch_tc(const CUtensorMap &ma, const CUtensorMap &mb, const GemmArgs &g, cudaStream_t s, int *err)
+int launch_tcp(const CUtensorMap &ma, const CUtensorMap &mb, const GemmArgs &g, cudaStream_t s, int *err)
 {
-    const size_t smem = tc_smem_bytes<BN>();
-    PCD_TRY(tc_attr<BN>());
-    const dim3 grid((g.N + BN - 1) / BN, (g.M + kTcBM - 1) / kTcBM, g.ksplit);
-    k_gemm_tc<BN><<<grid, kTcThreads, smem, s>>>(ma, mb, g, err);
+    PCD_TRY(tcp_attr<BN>());
+    const unsigned stride = tp_stride(g, BN);
+    const int nst = (int)std::min<unsigned>(kTpMaxStages, tp_ring_budget(BN) / stride);
+    const size_t smem = (size_t)nst * stride + kTpStageBytes + 1024;
+    const long units = (long)((g.M + kTcBM - 1) / kTcBM) * ((g.N + BN - 1) / BN) * g.ksplit;
+    const int grid = (int)std::max<long>(1, std::min<long>(units, (long)tp_ctas_per_sm(BN) * sm_count()));
+    k_gemm_tcp<BN><<<grid, kTpThreads, smem, s>>>(ma, mb, g, nst, err);
     PCD_LAUNCHED(1);
     return PCD_OK;
 }
@@ -631,10 +699,10 @@ int gemm_tc(const GemmArgs &g, cudaStream_t s)
         set_error("tcgen05 gemm: no error word");
         return PCD_DEVICE_ERROR;
     }
-    if (BN == 32) return launch_tc<32>(ma, mb, g, s, err);
-    if (BN == 64) return launch_tc<64>(ma, mb, g, s, err);
-    if (BN == 128) return launch_tc<128>(ma, mb, g, s, err);
-    return launch_tc<256>(ma, mb, g, s, err);
+    if (BN == 32) return launch_tcp<32>(ma, mb, g, s, err);
+    if (BN == 64) return launch_tcp<64>(ma, mb, g, s, err);
+    if (BN == 128) return launch_tcp<128>(ma, mb, g, s, err);
+    return launch_tcp<256>(ma, mb, g, s, err);
 }
 
 int gemm_tc_prepare()
@@ -643,10 +711,10 @@ int gemm_tc_prepare()
         set_error("tcgen05 gemm: no error word");
         return PCD_DEVICE_ERROR;
     }
-    PCD_TRY(tc_attr<32>());
-    PCD_TRY(tc_attr<64>());
-    PCD_TRY(tc_attr<128>());
-    PCD_TRY(tc_attr<256>());
+    PCD_TRY(tcp_attr<32>());
+    PCD_TRY(tcp_attr<64>());
+    PCD_TRY(tcp_attr<128>());
+    PCD_TRY(tcp_attr<256>());
     if (!encode_fn()) {
         set_error("tcgen05 gemm: cuTensorMapEncodeTiled is not available");
         return PCD_DEVICE_ERROR;

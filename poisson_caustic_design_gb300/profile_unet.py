@@ -2,12 +2,13 @@
 profiler captures (each run is deterministic and small enough for a
 full-metric capture of a few launches).
 
-    python -m poisson_caustic_design_gb300.profile_unet gemm [--time]
-        the tcgen05 GEMM on three U-Net contraction shapes (M x N x K):
-        131072 x 32 x 288 (first 32->32 conv at 64^2 x 32), 32768 x 64 x 576
-        (64->64 conv at 32^2 x 32), 16384 x 256 x 2304 (bottom 256->256 conv at
-        32^2 x 16); with --time, CUDA-event medians (L2 flushed between
-        launches) on the tcgen05 and the mma.sync kernels
+    python -m poisson_caustic_design_gb300.profile_unet gemm [--time] [--paths 2,3,1]
+        the GEMM on three U-Net contraction shapes (M x N x K): 131072 x 32 x
+        288 (first 32->32 conv at 64^2 x 32), 32768 x 64 x 576 (64->64 conv at
+        32^2 x 32), 16384 x 256 x 2304 (bottom 256->256 conv at 32^2 x 16), one
+        launch per shape and path (2: tcgen05, 1: mma.sync, 9: torch.matmul as
+        a timing reference; default 2); --shape M,N,K replaces the shapes; with --time, CUDA-event medians
+        (L2 flushed between launches)
     python -m poisson_caustic_design_gb300.profile_unet train R B STEPS [--path P]
         STEPS training steps of a resolution-R network on batch B (seeded
         random inputs); with --time, the CUDA-event mean of the steps after the
@@ -39,30 +40,38 @@ def _median_ms(fn, reps=20):
     return ts[len(ts) // 2]
 
 
-def gemm(timed: bool) -> dict:
+def gemm(timed: bool, paths=(2,), shapes=SHAPES) -> dict:
     import torch
 
     from . import _lib
 
     L = _lib.load()
     out = {}
-    for M, N, K in SHAPES:
+    for M, N, K in shapes:
         g = torch.Generator(device="cpu").manual_seed(M + N + K)
         A = torch.randn(M, K, generator=g).to(torch.bfloat16).cuda()
         B = torch.randn(N, K, generator=g).to(torch.bfloat16).cuda()
         C = torch.empty(M, N, dtype=torch.float32, device="cuda")
         s = torch.cuda.current_stream().cuda_stream
-        for path in ((2, 1) if timed else (2,)):
-            def run():
-                st = L.pcd_gemm_bf16_path(A.data_ptr(), K, B.data_ptr(), K, C.data_ptr(), N, M, N, K, 1, None, path, s)
-                if st != 0:
-                    raise RuntimeError(L.pcd_last_error())
+        for path in paths:
+            if path == 9:  # cuBLAS through torch (BF16 out), a timing reference only
+                def run():
+                    torch.matmul(A, B.T)
+            else:
+                def run():
+                    st = L.pcd_gemm_bf16_path(A.data_ptr(), K, B.data_ptr(), K, C.data_ptr(), N, M, N, K, 1, None, path,
+                                              s)
+                    if st != 0:
+                        raise RuntimeError(L.pcd_last_error())
 
             run()
             torch.cuda.synchronize()
+            if path == 9:
+                out[f"{M}x{N}x{K}_torch_ms"] = _median_ms(run) if timed else None
+                continue
             ref = A.float() @ B.float().T
             err = (C - ref).abs().max().item() / ref.abs().max().item()
-            if err > 1e-5:
+            if err > 1e-5 * max(1.0, (K / 1024) ** 0.5):  # FP32 sums in another order drift with sqrt(K)
                 raise RuntimeError(f"{M}x{N}x{K} path {path}: relative error {err}")
             if timed:
                 ms = _median_ms(run)
@@ -107,6 +116,8 @@ def main(argv=None):
     sub = ap.add_subparsers(dest="what", required=True)
     a = sub.add_parser("gemm")
     a.add_argument("--time", action="store_true")
+    a.add_argument("--paths", default="2")
+    a.add_argument("--shape", action="append", default=None, help="M,N,K (repeatable; default the three shapes)")
     b = sub.add_parser("train")
     b.add_argument("R", type=int)
     b.add_argument("B", type=int)
@@ -115,7 +126,8 @@ def main(argv=None):
     b.add_argument("--time", action="store_true")
     args = ap.parse_args(argv)
     if args.what == "gemm":
-        res = gemm(args.time)
+        shapes = tuple(tuple(int(v) for v in s.split(",")) for s in args.shape) if args.shape else SHAPES
+        res = gemm(args.time, tuple(int(p) for p in args.paths.split(",")), shapes)
     else:
         res = train(args.R, args.B, args.steps, args.path, args.time)
     print(json.dumps(res))

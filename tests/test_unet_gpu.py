@@ -35,13 +35,15 @@ def test_gemm_matches_torch(M, N, K, ksplit):
 
 @pytest.mark.parametrize("M,N,K,ksplit", [(512, 128, 64, 1), (300, 96, 96, 1), (4096, 32, 288, 1), (1000, 256, 576, 2),
                                           (130, 700, 160, 3), (8192, 64, 2304, 1), (16384, 128, 1152, 1),
-                                          (2048, 256, 2304, 1), (700, 300, 192, 2)])
+                                          (2048, 256, 2304, 1), (700, 300, 192, 2), (131072, 32, 288, 1),
+                                          (20000, 96, 640, 3)])
 def test_gemm_tcgen05_matches_torch(M, N, K, ksplit):
     """The tcgen05 GEMM (TMA loads with the 128-byte swizzle, tcgen05.mma into
-    a tensor-memory accumulator, tcgen05.ld epilogue) against torch: tails in
-    M, N and K (K not a multiple of the 64-wide K tile, N below the N tile),
-    split-K, and the U-Net's convolution shapes; the mma.sync path on the same
-    inputs agrees too."""
+    tensor-memory accumulators, tcgen05.ld epilogue; persistent CTAs) against
+    torch: tails in M, N and K (K not a multiple of the 64-wide K tile, N
+    below the N tile), split-K, the U-Net's convolution shapes, and grids of
+    several tiles per persistent CTA (both accumulators in turn); the
+    mma.sync path on the same inputs agrees too."""
     import torch
 
     from poisson_caustic_design_gb300 import _lib
