@@ -716,8 +716,8 @@ int relu_bwd_colsum(const float *dY, int lddy, const __nv_bfloat16 *Y, int ldy, 
         PCD_TRY(relu_bwd(dY, lddy, Y, ldy, P, C, relu, dYm, s));
         return colsum(dYm, P, C, part, db, s);
     }
-    // about 128 pixels per block, at most 1024 blocks (and what part holds)
-    const int chunks = (int)std::max<long>(1, std::min<long>(std::min<long>((P + 127) / 128, 1024), part_cap / C));
+    // about 4096 values (16 a thread) per block, at most 1024 blocks (and what part holds)
+    const int chunks = (int)std::max<long>(1, std::min<long>(std::min<long>((P * C + 4095) / 4096, 1024), part_cap / C));
     k_relu_bwd_colsum<<<chunks, kThreads, 0, s>>>(dY, lddy, Y, ldy, P, C, relu, dYm, part, chunks);
     PCD_LAUNCHED(1);
     k_colsum_fold_warp<<<(C + 7) / 8, 256, 0, s>>>(part, chunks, C, db);

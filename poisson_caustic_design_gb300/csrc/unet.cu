@@ -311,16 +311,30 @@ static long tc_tiles(long P, int N)
     return ((P + 127) / 128) * ((N + bn - 1) / bn);
 }
 
+// K splits for an implicit convolution on the tcgen05 kernel whose output
+// tiles do not fill the chip: enough for about one unit per SM, at most the
+// K tiles (taps x channel chunks) and what the partial buffer holds
+int UNet::conv_splits(long P, int N, int Cin) const
+{
+    const long tiles = tc_tiles(P, N), sms = nn::sm_count();
+    if (tiles >= sms) return 1;
+    const int kt = 9 * (Cin == 32 ? 1 : (Cin + 63) / 64);
+    int ks = (int)std::min<long>(std::min<long>((sms + tiles - 1) / tiles, kt), 16);
+    while (ks > 1 && (size_t)ks * P * N > partials_cap) ks /= 2;
+    return std::max(1, ks);
+}
+
 int UNet::conv_fwd(Conv &c, int B, cudaStream_t s)
 {
-    // an implicit GEMM on the tcgen05 kernel (no im2col matrix) where its
-    // tiles fill the chip; otherwise im2col and the GEMM (split-K for small grids)
+    // an implicit GEMM on the tcgen05 kernel (no im2col matrix; split-K where
+    // its tiles do not fill the chip); otherwise im2col and the GEMM
     const long P = (long)B * c.S * c.S;
     c.col_valid = false;
-    if (nn::default_path() == 0 && c.Kp == 9 * c.Cin && nn::conv_tc_applies(c.in, B, c.S, c.S, c.Cin, c.ldin, 128) &&
-        tc_tiles(P, c.Cout) >= nn::sm_count())
+    if (nn::default_path() == 0 && c.Kp == 9 * c.Cin && nn::conv_tc_applies(c.in, B, c.S, c.S, c.Cin, c.ldin, 128)) {
+        const int ks = conv_splits(P, c.Cout, c.Cin);
         return nn::conv3x3_tc(c.in, B, c.S, c.S, c.Cin, c.ldin, c.wb, c.Kp, c.Cout, params_f + c.off_b, c.relu, c.out,
-                              nullptr, c.ldout, 1, nullptr, s);
+                              nullptr, c.ldout, ks, partials, s);
+    }
     PCD_TRY(nn::im2col(c.in, B, c.S, c.S, c.Cin, c.ldin, c.col, c.Kp, s));
     c.col_valid = true;
     nn::GemmArgs g{};
@@ -447,13 +461,12 @@ int UNet::conv_bwd(Conv &c, int B, const float *dY, int lddy, float *dX, cudaStr
         PCD_TRY(nn::gemm(g, s, partials));
     }
     if (dX) {
-        // dX = conv(dYm, flipped weights): implicit on the tcgen05 kernel
-        // where its tiles fill the chip, else through im2col
+        // dX = conv(dYm, flipped weights): implicit on the tcgen05 kernel,
+        // else through im2col
         PCD_TRY(nn::flip(c.wb, c.Cout, c.Cin, c.Kp, wflip, c.Kpf, s));
-        if (nn::default_path() == 0 && c.Kpf == 9 * c.Cout && nn::conv_tc_applies(dym, B, c.S, c.S, c.Cout, c.Cout, 128) &&
-            tc_tiles(P, c.Cin) >= sms)
-            return nn::conv3x3_tc(dym, B, c.S, c.S, c.Cout, c.Cout, wflip, c.Kpf, c.Cin, nullptr, 0, nullptr, dX, c.Cin, 1,
-                                  nullptr, s);
+        if (nn::default_path() == 0 && c.Kpf == 9 * c.Cout && nn::conv_tc_applies(dym, B, c.S, c.S, c.Cout, c.Cout, 128))
+            return nn::conv3x3_tc(dym, B, c.S, c.S, c.Cout, c.Cout, wflip, c.Kpf, c.Cin, nullptr, 0, nullptr, dX, c.Cin,
+                                  conv_splits(P, c.Cin, c.Cout), partials, s);
         PCD_TRY(nn::im2col(dym, B, c.S, c.S, c.Cout, c.Cout, colD, c.Kpf, s));
         nn::GemmArgs d{};
         d.A = colD;

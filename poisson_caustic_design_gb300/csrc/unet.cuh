@@ -39,6 +39,7 @@ struct UNet {
     int load_input(const float *x, int B, cudaStream_t s);
     int forward(int B, cudaStream_t s);
     int backward(int B, cudaStream_t s);
+    int conv_splits(long P, int N, int Cin) const;
     int conv_fwd(Conv &c, int B, cudaStream_t s);
     int conv_bwd(Conv &c, int B, const float *dY, int lddy, float *dX, cudaStream_t s);
 };

@@ -298,8 +298,10 @@ def test_unet_forward_and_gradients_match_torch(ctx):
             rel = np.linalg.norm(go - gt) / nt
             cos = float(go @ gt / (np.linalg.norm(go) * nt + 1e-30))
             assert rel < rel_tol and cos > cos_tol, (name, rel, cos)
-    # the weight gradients through the transposes and the mma.sync kernel
-    # (the GEMM pinned to mma.sync) agree with the MN-major tcgen05 form
+    # the whole step pinned to the mma.sync kernel (im2col, transposes) agrees
+    # with the tcgen05 forms (implicit convolutions, MN-major weight
+    # gradients) to BF16 rounding: the two forward passes round their BF16
+    # activations after sums in different orders
     L = net._L
     assert L.pcd_gemm_set_default_path(1) == 0
     try:
@@ -312,7 +314,7 @@ def test_unet_forward_and_gradients_match_torch(ctx):
             continue
         n = g16[name].size
         rel = np.linalg.norm(g1[off:off + n] - g[off:off + n]) / np.linalg.norm(g[off:off + n])
-        assert rel < 1e-4, (name, rel)
+        assert rel < 5e-3, (name, rel)
     net.close()
 
 
