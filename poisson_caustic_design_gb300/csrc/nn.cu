@@ -182,6 +182,8 @@ __global__ void __launch_bounds__(GTHREADS) k_gemm(GemmArgs g)
 }
 
 // sum of split-K partials in a fixed order, + bias, ReLU, store
+// C = sum over the K splits of part[z][m][n] (+ bias, ReLU), one thread per
+// output (few splits, many outputs)
 __global__ void k_splitk_reduce(const float *part, int splits, int M, int N, int ldc, const float *bias, int relu,
                                 __nv_bfloat16 *Cb, float *Cf, int ldo)
 {
@@ -197,7 +199,51 @@ __global__ void k_splitk_reduce(const float *part, int splits, int M, int N, int
     }
 }
 
-inline int grid1d(long n, int t = 256) { return (int)std::max<long>(1, std::min<long>(8192, (n + t - 1) / t)); }
+// The same for many splits over few outputs (the weight gradients): a block
+// of 32 x 8 threads takes 32 consecutive outputs, thread (x, y) adds splits
+// y, y + 8, ..., and column x's eight sums fold in a fixed order.
+constexpr int kReduceLanes = 8, kReduceLanesFrom = 16;
+__global__ void k_splitk_reduce_lanes(const float *part, int splits, int M, int N, int ldc, const float *bias, int relu,
+                                __nv_bfloat16 *Cb, float *Cf, int ldo)
+{
+    __shared__ float red[kReduceLanes][33];
+    const long total = (long)M * N;
+    for (long t0 = (long)blockIdx.x * 32; t0 < total; t0 += (long)gridDim.x * 32) {
+        const long t = t0 + threadIdx.x;
+        const int m = (int)(t / N), n = (int)(t - (long)m * N);
+        float v = 0.f;
+        if (t < total)
+            for (int z = threadIdx.y; z < splits; z += kReduceLanes) v += part[((size_t)z * M + m) * ldc + n];
+        red[threadIdx.y][threadIdx.x] = v;
+        __syncthreads();
+        if (threadIdx.y == 0 && t < total) {
+            for (int y = 1; y < kReduceLanes; y++) v += red[y][threadIdx.x];
+            if (bias) v += bias[n];
+            if (relu) v = fmaxf(v, 0.f);
+            if (Cb) Cb[(size_t)m * ldo + n] = __float2bfloat16(v);
+            else Cf[(size_t)m * ldo + n] = v;
+        }
+        __syncthreads();
+    }
+}
+
+inline int reduce_blocks(long outputs) { return (int)std::max<long>(1, std::min<long>(16384, (outputs + 31) / 32)); }
+
+inline int grid1d(long n, int t = 256);
+
+// out = the split-K partials' sum: the per-output form for few splits, the
+// 8-lane form from kReduceLanesFrom splits on
+void splitk_reduce(const float *part, int splits, int M, int N, int ldc, const float *bias, int relu,
+                   __nv_bfloat16 *Cb, float *Cf, int ldo, cudaStream_t s)
+{
+    if (splits >= kReduceLanesFrom)
+        k_splitk_reduce_lanes<<<reduce_blocks((long)M * N), dim3(32, kReduceLanes), 0, s>>>(part, splits, M, N, ldc,
+                                                                                           bias, relu, Cb, Cf, ldo);
+    else
+        k_splitk_reduce<<<grid1d((long)M * N), 256, 0, s>>>(part, splits, M, N, ldc, bias, relu, Cb, Cf, ldo);
+}
+
+inline int grid1d(long n, int t) { return (int)std::max<long>(1, std::min<long>(8192, (n + t - 1) / t)); }
 
 // im2col of an NHWC activation slice: out[p][tap*C + c] (zeros outside the
 // image and for k >= 9C up to Kp)
@@ -662,12 +708,10 @@ int gemm(const GemmArgs &g0, cudaStream_t s, float *partials)
     if (!tc) PCD_LAUNCHED(1);
     if (g.ksplit > 1 && g.trans_c) {
         // the transposed partials reduce as an N x M matrix into C[n][m]
-        k_splitk_reduce<<<grid1d((long)Mo * g.N), 256, 0, s>>>(partials, g.ksplit, g.N, Mo, Mo, nullptr, 0, nullptr,
-                                                              outF, ldo);
+        splitk_reduce(partials, g.ksplit, g.N, Mo, Mo, nullptr, 0, nullptr, outF, ldo, s);
         PCD_LAUNCHED(1);
     } else if (g.ksplit > 1) {
-        k_splitk_reduce<<<grid1d((long)g.M * g.N), 256, 0, s>>>(partials, g.ksplit, g.M, g.N, g.N, g.bias, g.relu,
-                                                               outB, outF, ldo);
+        splitk_reduce(partials, g.ksplit, g.M, g.N, g.N, g.bias, g.relu, outB, outF, ldo, s);
         PCD_LAUNCHED(1);
     }
     return PCD_OK;
