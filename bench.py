@@ -499,6 +499,44 @@ def config0_section(pcd, ctx, device, batch=16):
     return out
 
 
+def config3_section(pcd, ctx, net, train_steps=12):
+    """The learned warm start on the held-out seeds (900000-900007, Gaussian
+    and binary densities): each solved to relative residual 1e-6 at 256^2 and
+    512^2 by the mixed form from a zero guess and from the network's judged
+    prediction (train_unet.evaluate), and the CUDA-event time of a training
+    step at the network's 64^2 grid and batch 32 (seeded random inputs)."""
+    import torch
+
+    from poisson_caustic_design_gb300 import learned as _learned
+    from poisson_caustic_design_gb300 import train_unet as _train
+
+    rows = _train.evaluate(ctx, net)
+    summ = _train.summarize(rows)
+    tnet = _learned.UNet(ctx, resolution=64, max_batch=32, seed=1)
+    g = torch.Generator(device="cpu").manual_seed(64)
+    x = torch.randn(32, 64, 64, generator=g).cuda()
+    t = torch.randn(32, 64, 64, generator=g).cuda()
+    tnet.train_step(x, t, 1e-4)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(train_steps):
+        tnet.train_step(x, t, 1e-4)
+    e1.record()
+    e1.synchronize()
+    tnet.close()
+    net.attach(ctx)
+    return {"held_out_seeds": [900000, 900007], "sizes": [256, 512], "tol": 1e-6,
+            "mean_sweep_ratio": summ["mean_sweep_ratio"], "mean_time_ratio": summ["mean_time_ratio"],
+            "accepted": summ["accepted"], "evaluated": summ["evaluated"],
+            "mean_ms": {str(n): {"zero_start": float(np.mean([r["ms_0"] for r in rows if r["n"] == n])),
+                                 "learned_start": float(np.mean([r["ms_2"] for r in rows if r["n"] == n]))}
+                        for n in (256, 512)},
+            "train_step_ms_64x32": e0.elapsed_time(e1) / train_steps,
+            "note": "ratios are learned + mixed over mixed from a zero guess; the network runs on the density "
+                    "area-averaged to 64^2 (BF16, tcgen05 tensor cores)"}
+
+
 def config4_section(pcd, ctx, device, batch=16):
     """The largest workload: mesh 1024^2 on 4096^2 grids.  `batch` targets
     (seeds 0..batch-1) initialised and taken through their first transport
@@ -763,6 +801,13 @@ def run_ours(args, rank, world, local, pg):
                                         "note": "per-sweep time of the reference's threaded SOR at 4096^2 times "
                                                 "the GPU's mean sweep count (one transport solve takes minutes)"}
 
+    # config 3: the learned warm start on held-out seeds at 256^2 and 512^2
+    # (learned + mixed against mixed from a zero guess, same tolerance), and
+    # one training step of the network at its training batch
+    config3 = None
+    if net is not None and not args.no_pipelines and not args.headline_only:
+        config3 = config3_section(pcd, ctx, net)
+
     cpu = None
     if rank == 0 and not args.no_cpu_baseline and not args.headline_only:
         # the reference's threaded solver on the same eight densities as the
@@ -798,6 +843,7 @@ def run_ours(args, rank, world, local, pg):
         "batched": batched,
         "config0_pipeline": config0,
         "config4_pipeline_batched": config4,
+        "config3_learned": config3,
         "roofline_stream_4096": stream_roof,
         "roofline": roof,
         "cpu_baseline": cpu,
