@@ -77,7 +77,8 @@ def test_gemm_tcgen05_operand_layouts_match_torch(M, N, K, ksplit, a_mn, b_mn, t
     [K][N]: the U-Net's weight gradient reads the im2col matrix and dY where
     they lie) and a transposed C, against torch: 64-wide MN blocks with the
     128-byte swizzle, a 32-wide B with the 64-byte swizzle, tails in M, N and
-    K, row strides wider than the matrix, split-K."""
+    K, row strides wider than the matrix, split-K, and a repeated launch
+    (bit-identical: the partials are summed in split order)."""
     import torch
 
     from poisson_caustic_design_gb300 import _lib
@@ -104,6 +105,14 @@ def test_gemm_tcgen05_operand_layouts_match_torch(M, N, K, ksplit, a_mn, b_mn, t
     assert err < 1e-5, err
     if trans_c:
         assert torch.isnan(C[:, M:]).all()  # nothing written beyond column M of C[n][:]
+    # again: the partials are summed in split order, so a second launch is
+    # bit-identical
+    C2 = torch.full_like(C, float("nan"))
+    st = L.pcd_gemm_bf16_layout(As.data_ptr(), lda, a_mn, Bs.data_ptr(), ldb, b_mn, C2.data_ptr(), ldc, trans_c, M, N,
+                                K, ksplit, part.data_ptr(), torch.cuda.current_stream().cuda_stream)
+    assert st == 0, L.pcd_last_error()
+    torch.cuda.synchronize()
+    assert torch.equal(torch.nan_to_num(C2, nan=7.0), torch.nan_to_num(C, nan=7.0))
 
 
 def _conv_case(B, H, W, C, ldx, off, N, seed):
