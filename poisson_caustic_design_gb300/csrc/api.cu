@@ -69,14 +69,19 @@ int judge_prepare(pcd_ctx *ctx, int W, int H, int ld, cudaStream_t s)
         if (J.zero) cudaFree(J.zero);
         if (J.mask) cudaFree(J.mask);
         if (J.mask_z) cudaFree(J.mask_z);
+        if (J.e32) cudaFree(J.e32);
+        if (J.r32) cudaFree(J.r32);
         J.b = J.pred = J.zero = nullptr;
         J.mask = J.mask_z = nullptr;
+        J.e32 = J.r32 = nullptr;
         J.cells = 0;
         PCD_CUDA(cudaMalloc(&J.b, cells * sizeof(double)));
         PCD_CUDA(cudaMalloc(&J.pred, cells * sizeof(double)));
         PCD_CUDA(cudaMalloc(&J.zero, cells * sizeof(double)));
         PCD_CUDA(cudaMalloc(&J.mask, cells));
         PCD_CUDA(cudaMalloc(&J.mask_z, cells));
+        PCD_CUDA(cudaMalloc(&J.e32, 2 * cells * sizeof(float)));
+        PCD_CUDA(cudaMalloc(&J.r32, 2 * cells * sizeof(float)));
         J.cells = cells;
     }
     if (!J.ctl) {
@@ -90,6 +95,15 @@ int judge_prepare(pcd_ctx *ctx, int W, int H, int ld, cudaStream_t s)
         PCD_CUDA(cudaEventCreateWithFlags(&J.join, cudaEventDisableTiming));
         PCD_CUDA(cudaStreamCreateWithFlags(&J.side, cudaStreamNonBlocking));
     }
+    // grids that fit one cluster smooth in the mixed form (FP64 residuals,
+    // FP32 sweeps on the cluster), others with FP64 half-sweep launches
+    J.mixed = smooth_mixed_applies(ctx->device, W, H);
+    auto smooth = [&](double *phi, uint8_t *mask, Ctl *ctl, double *partials, int branch, cudaStream_t st) {
+        if (J.mixed)
+            return enqueue_smooth_mixed(J.b, phi, J.e32 + (size_t)branch * cells, J.r32 + (size_t)branch * cells, ctl,
+                                        partials, W, H, ld, kLearnedSmooth, ctx->device, st);
+        return enqueue_smooth(J.b, phi, mask, ctl, partials, W, H, ld, kLearnedSmooth, 1.0, st);
+    };
     const unsigned long long n0 = g_launches.load();
     cudaGraph_t g;
     PCD_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
@@ -99,12 +113,10 @@ int judge_prepare(pcd_ctx *ctx, int W, int H, int ld, cudaStream_t s)
                  ? PCD_OK
                  : PCD_DEVICE_ERROR;
     if (st == PCD_OK) st = zero_grid(J.zero, W, H, ld, J.side);
-    if (st == PCD_OK)
-        st = enqueue_smooth(J.b, J.zero, J.mask_z, J.ctl, J.partials_z, W, H, ld, kLearnedSmooth, 1.0, J.side);
+    if (st == PCD_OK) st = smooth(J.zero, J.mask_z, J.ctl, J.partials_z, 0, J.side);
     if (st == PCD_OK && cudaEventRecord(J.join, J.side) != cudaSuccess) st = PCD_DEVICE_ERROR;
     if (st == PCD_OK) st = net.warm_start(J.b, W, H, ld, J.pred, s);
-    if (st == PCD_OK)
-        st = enqueue_smooth(J.b, J.pred, J.mask, J.ctl + 1, J.partials, W, H, ld, kLearnedSmooth, 1.0, s);
+    if (st == PCD_OK) st = smooth(J.pred, J.mask, J.ctl + 1, J.partials, 1, s);
     if (st == PCD_OK && cudaStreamWaitEvent(s, J.join, 0) != cudaSuccess) st = PCD_DEVICE_ERROR;
     if (st == PCD_DEVICE_ERROR) set_error("judge graph: fork / join of the capture failed");
     const cudaError_t ce = cudaStreamEndCapture(s, &g);
@@ -144,6 +156,8 @@ void JudgeGraph::release()
     if (zero) cudaFree(zero);
     if (mask) cudaFree(mask);
     if (mask_z) cudaFree(mask_z);
+    if (e32) cudaFree(e32);
+    if (r32) cudaFree(r32);
     if (ctl) cudaFree(ctl);
     if (partials) cudaFree(partials);
     if (partials_z) cudaFree(partials_z);

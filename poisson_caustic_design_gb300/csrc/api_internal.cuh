@@ -43,8 +43,10 @@ struct JudgeOut {
 };
 
 // The learned warm start and its judge (prediction, kLearnedSmooth Gauss-
-// Seidel sweeps on it and on a zero guess, both FP64 residuals) as one CUDA
-// graph per grid shape and network, on buffers of its own: the caller's b is
+// Seidel sweeps on it and on a zero guess -- FP32 sweeps on one cluster with
+// the residuals in FP64 where the grid fits one cluster, FP64 half-sweep
+// launches otherwise -- and both FP64 residuals) as one CUDA graph per grid
+// shape and network, on buffers of its own: the caller's b is
 // copied in before the replay and the chosen start copied out after it, so a
 // solve with the learned warm start has no host round trip before the solver.
 struct JudgeGraph {
@@ -55,6 +57,8 @@ struct JudgeGraph {
     size_t cells = 0;
     double *b = nullptr, *pred = nullptr, *zero = nullptr, *partials = nullptr, *partials_z = nullptr;
     uint8_t *mask = nullptr, *mask_z = nullptr;
+    float *e32 = nullptr, *r32 = nullptr;  // [2 * cells]: the mixed smoothing's correction and RHS per branch
+    bool mixed = false;                   // the graph smooths in the mixed form (one cluster, FP32 sweeps)
     cudaStream_t side = nullptr;    // the zero guess's branch of the capture
     cudaEvent_t fork = nullptr, join = nullptr;
     Ctl *ctl = nullptr;             // [2]: zero guess, prediction

@@ -1083,6 +1083,58 @@ int enqueue_smooth(const double *b, double *phi, uint8_t *mask, Ctl *ctl, double
     return PCD_OK;
 }
 
+int enqueue_smooth_mixed(const double *b, double *phi, float *e32, float *r32, Ctl *ctl, double *partials, int W,
+                         int H, int ld, int sweeps, int dev, cudaStream_t s)
+{
+    ClusterPlan plan{};
+    if (cluster_plan(dev, W, H, 4, &plan) != PCD_OK) {
+        set_error("mixed smoothing: the grid does not fit one cluster");
+        return PCD_BAD_ARG;
+    }
+    SolveArgs a{};
+    a.W = W; a.H = H; a.ld = ld;
+    a.stop = PCD_STOP_REL_RESIDUAL;
+    a.max_iter = sweeps;
+    a.tol = 0.0;
+    a.omega = 1.0;
+    for (int c = 0; c < 5; c++) {
+        a.w64[c] = 1.0 / (double)c;
+        a.w32[c] = 1.0f / (float)c;
+    }
+    PCD_CUDA(cudaMemsetAsync(ctl, 0, sizeof(Ctl), s));
+    PCD_CUDA(cudaMemsetAsync(e32, 0, sizeof(float) * (size_t)H * ld, s));
+    const int rblocks = grid_blocks((long)W * H);
+    // r32 = b - L phi and ||b|| (FP64)
+    k_refine_residual<false><<<rblocks, kThreads, 0, s>>>(phi, e32, b, nullptr, r32, ctl, partials, a, 1);
+    PCD_LAUNCHED(1);
+    // `sweeps` FP32 Gauss-Seidel sweeps of L e = r32 on one cluster (no
+    // estimates, no early end: tolerance 0, drop 0, one cycle of `sweeps`)
+    ClusterArgs ca{};
+    ca.W = W; ca.H = H; ca.ld = ld; ca.khp = plan.khp;
+    ca.e = e32; ca.r32 = r32; ca.ctl = ctl;
+    ca.check_every = sweeps + 1;
+    ca.cycle_cap = sweeps;
+    ca.max_iter = sweeps;
+    ca.tol = 0.0;
+    ca.drop = 0.0;
+    for (int c = 0; c < 5; c++) ca.w32[c] = a.w32[c];
+    ca.one_minus_omega = 0.0f;
+    ca.depth = plan.depth;
+    PCD_TRY(launch_cluster(ca, plan, s));
+    // ||b - L (phi + e)|| / ||b|| in FP64 into ctl->rel, then phi += e
+    k_refine_residual<false><<<rblocks, kThreads, 0, s>>>(phi, e32, b, nullptr, r32, ctl, partials, a, 0);
+    PCD_LAUNCHED(1);
+    k_refine_update<<<rblocks, kThreads, 0, s>>>(phi, e32, ctl, a);
+    PCD_LAUNCHED(1);
+    return PCD_OK;
+}
+
+bool smooth_mixed_applies(int dev, int W, int H)
+{
+    ClusterPlan plan{};
+    return cluster_plan(dev, W, H, 4, &plan) == PCD_OK;
+}
+
 size_t residual_partials_bytes() { return sizeof(double) * 3 * kResidualBlocksMax; }
 
 int smooth_residual(SolverWorkspace &ws, const double *b, double *phi, int W, int H, int ld, int sweeps, double omega,

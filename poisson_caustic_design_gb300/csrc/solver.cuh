@@ -154,6 +154,14 @@ int smooth_residual(SolverWorkspace &ws, const double *b, double *phi, int W, in
 int enqueue_smooth(const double *b, double *phi, uint8_t *mask, Ctl *ctl, double *partials, int W, int H, int ld,
                    int sweeps, double omega, cudaStream_t s);
 size_t residual_partials_bytes();
+// The same smoothing (Gauss-Seidel, omega = 1) in the mixed form: r = b - L
+// phi in FP64, `sweeps` FP32 sweeps of L e = r on one thread-block cluster,
+// then ||b - L (phi + e)|| / ||b|| in FP64 into ctl->rel and phi += e; for
+// grids that fit one cluster (smooth_mixed_applies) and have no NaN cells
+// (a NaN in b makes rel NaN).  e32, r32: H * ld floats.  Capturable.
+int enqueue_smooth_mixed(const double *b, double *phi, float *e32, float *r32, Ctl *ctl, double *partials, int W,
+                         int H, int ld, int sweeps, int dev, cudaStream_t s);
+bool smooth_mixed_applies(int dev, int W, int H);
 
 int solve_device(SolverWorkspace &ws, const double *b, double *phi, int W, int H, int ld,
                  const pcd_solve_opts &o, pcd_solve_stats *stats, cudaStream_t s);
