@@ -9,6 +9,13 @@ full-metric capture of a few launches).
         launch per shape and path (2: tcgen05, 1: mma.sync, 9: torch.matmul as
         a timing reference; default 2); --shape M,N,K replaces the shapes; with --time, CUDA-event medians
         (L2 flushed between launches)
+    python -m poisson_caustic_design_gb300.profile_unet conv [--time]
+        the 3x3 convolution as an implicit GEMM on the tcgen05 kernel (no
+        im2col; 4-D TMA boxes of the NHWC input per tap) on two U-Net layers:
+        32 -> 32 channels at 256^2 x 16 and 128 -> 128 at 64^2 x 16, one launch
+        each; with --time, CUDA-event medians (L2 flushed) beside torch's
+        conv2d on the same BF16 data (cuDNN, NCHW channels-last, a timing
+        reference only)
     python -m poisson_caustic_design_gb300.profile_unet train R B STEPS [--path P]
         STEPS training steps of a resolution-R network on batch B (seeded
         random inputs); with --time, the CUDA-event mean of the steps after the
@@ -81,6 +88,48 @@ def gemm(timed: bool, paths=(2,), shapes=SHAPES) -> dict:
     return out
 
 
+CONVS = ((16, 256, 256, 32, 32), (16, 64, 64, 128, 128))  # batch, height, width, Cin, Cout
+
+
+def conv(timed: bool) -> dict:
+    import torch
+    import torch.nn.functional as F
+
+    from . import _lib
+
+    L = _lib.load()
+    out = {}
+    for B, H, W, C, N in CONVS:
+        g = torch.Generator(device="cpu").manual_seed(B + H + C)
+        x = torch.randn(B, H, W, C, generator=g).to(torch.bfloat16).cuda()
+        w = torch.randn(N, 9 * C, generator=g).to(torch.bfloat16).cuda()
+        y = torch.empty(B * H * W, N, dtype=torch.float32, device="cuda")
+        s = torch.cuda.current_stream().cuda_stream
+
+        def run():
+            st = L.pcd_conv3x3_bf16(x.data_ptr(), B, H, W, C, C, w.data_ptr(), 9 * C, N, y.data_ptr(), N, s)
+            if st != 0:
+                raise RuntimeError(L.pcd_last_error())
+
+        run()
+        torch.cuda.synchronize()
+        xt = x.permute(0, 3, 1, 2)  # NCHW view of the NHWC data (channels-last)
+        wt = w.reshape(N, 3, 3, C).permute(0, 3, 1, 2).contiguous(memory_format=torch.channels_last)
+        ref = F.conv2d(xt.float(), wt.float(), padding=1).permute(0, 2, 3, 1).reshape(B * H * W, N)
+        err = (y - ref).abs().max().item() / ref.abs().max().item()
+        if err > 1e-5:
+            raise RuntimeError(f"conv {B}x{H}x{W}x{C}->{N}: relative error {err}")
+        key = f"{B}x{H}x{W}_{C}to{N}"
+        if timed:
+            ms = _median_ms(run)
+            tms = _median_ms(lambda: F.conv2d(xt, wt, padding=1))
+            out[key] = {"ms": ms, "tflops": 2.0 * B * H * W * N * 9 * C / ms / 1e9, "torch_ms": tms,
+                        "bytes_in_out": B * H * W * (2 * C + 4 * N)}
+    if L.pcd_gemm_bf16_status() != 0:
+        raise RuntimeError(L.pcd_last_error())
+    return out
+
+
 def train(R: int, B: int, steps: int, path: int, timed: bool) -> dict:
     import torch
 
@@ -118,6 +167,8 @@ def main(argv=None):
     a.add_argument("--time", action="store_true")
     a.add_argument("--paths", default="2")
     a.add_argument("--shape", action="append", default=None, help="M,N,K (repeatable; default the three shapes)")
+    c = sub.add_parser("conv")
+    c.add_argument("--time", action="store_true")
     b = sub.add_parser("train")
     b.add_argument("R", type=int)
     b.add_argument("B", type=int)
@@ -125,7 +176,9 @@ def main(argv=None):
     b.add_argument("--path", type=int, default=0)
     b.add_argument("--time", action="store_true")
     args = ap.parse_args(argv)
-    if args.what == "gemm":
+    if args.what == "conv":
+        res = conv(args.time)
+    elif args.what == "gemm":
         shapes = tuple(tuple(int(v) for v in s.split(",")) for s in args.shape) if args.shape else SHAPES
         res = gemm(args.time, tuple(int(p) for p in args.paths.split(",")), shapes)
     else:
