@@ -26,10 +26,10 @@ namespace nn {
 namespace {
 
 constexpr int GBM = 128, GBK = 32, GST = 3, GTHREADS = 256;
-// automatic path: the tcgen05 form (nn_tc.cu) for every GEMM it takes whose
-// output tiles fill the chip (a whole U-Net pass at 256^2 x 16: inference 7%
-// and a training step 13% faster than on mma.sync; at 64^2 x 1, where every
-// GEMM has 32 tiles or fewer, mma.sync is 13% faster), unless pinned to mma.sync
+// automatic path for a plain GEMM: the tcgen05 form (nn_tc.cu) when it takes
+// it and its output tiles fill the chip, else mma.sync; 1 pins everything,
+// the U-Net's implicit convolutions included, to mma.sync (the convolutions
+// choose the tcgen05 form themselves, with split-K on small grids)
 std::atomic<int> g_default_path{0};
 constexpr int SROW = GBK + 8;  // padded shared row: 40 bf16 = 80 bytes
 

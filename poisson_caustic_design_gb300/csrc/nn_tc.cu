@@ -663,10 +663,10 @@ static int tc_bn(int N) { return N <= 32 ? 32 : (N <= 64 ? 64 : (N <= 128 ? 128 
 
 bool gemm_tc_fills_chip(const GemmArgs &g)
 {
-    // Below one CTA per SM the per-CTA set-up (tensor-memory allocation,
-    // barrier initialisation, the tensor maps' fetch) and the single issuing
-    // thread's latency are not hidden: at 64^2 pixels and batch 1 the U-Net's
-    // GEMMs (32 tiles and fewer) run faster on the mma.sync kernel.
+    // Below one output tile per SM a plain GEMM gains nothing from the
+    // persistent form's overlap and pays its set-up (tensor-memory
+    // allocation, barrier initialisation, the tensor maps' fetch); such
+    // GEMMs stay on the mma.sync kernel unless the caller asks for tcgen05.
     static int sms = 0;
     if (!sms) {
         int dev = 0, n = 0;
