@@ -229,8 +229,11 @@ __global__ void k_areas_errors(const double2 *__restrict__ tp, const double *__r
 }
 
 // ---- target areas (initialisation) ----------------------------------------
-// Clip a convex polygon against s*(coord[axis] - c) >= 0.
-__device__ __forceinline__ int clip_half(const double2 *in, int n, double2 *out, int axis, double c, double s)
+// Clip a convex polygon against s*(coord[axis] - c) >= 0.  Not inlined: its
+// four call sites per pixel, each with the FP64 division's code, made the
+// kernel wait on instruction fetch (no_instruction the first stall at 81 per
+// issue); one shared copy runs the initialisation 22% faster.
+__device__ __noinline__ int clip_half(const double2 *in, int n, double2 *out, int axis, double c, double s)
 {
     int m = 0;
     for (int k = 0; k < n; k++) {
