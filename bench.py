@@ -889,9 +889,50 @@ def run_pipeline_profile(local):
         out[name + "_ms"] = (time.perf_counter() - t) * 1e3
         if name != "init":
             out[name + "_solve_ms"] = d.last_solve_stats["device_ms"]
+    # the steps around the solve at the same size: image ingest (a 1024^2
+    # 8-bit PNG decoded, resized to the 4096^2 grid on the GPU), fold handling
+    # (one Laplacian smoothing of the target mesh, the fold count), the
+    # output files (the target solid as OBJ, the parameterisation as SVG)
+    import tempfile
+
+    from poisson_caustic_design_gb300 import image as _image
+
+    png = _gray_png(np.clip(np.round(_image.resize_image(img, R, R)), 0, 255).astype(np.uint8))
+    steps = {"png_decode_1024": lambda: _image.png_decode(png),
+             "resize_1024_to_4096": lambda: _image.resize_image(img[::4, ::4], N, N),
+             "smooth_target_mesh": lambda: d.smooth_target_mesh(0.5),
+             "count_folds": d.count_folds}
+    with tempfile.TemporaryDirectory() as td:
+        steps["save_solid_obj_target"] = lambda: d.save_solid_obj_target(os.path.join(td, "target.obj"))
+        steps["export_parameterization_svg"] = lambda: d.export_paramererization_to_svg(os.path.join(td, "p.svg"),
+                                                                                         0.5)
+        for name, fn in steps.items():
+            fn()  # first use (allocations, page cache)
+            torch.cuda.synchronize()
+            t = time.perf_counter()
+            fn()
+            torch.cuda.synchronize()
+            out[name + "_ms"] = (time.perf_counter() - t) * 1e3
+    out["png_bytes"] = len(png)
     print(json.dumps({"pipeline_profile": out}), flush=True)
     d.close()
     ctx.close()
+
+
+def _gray_png(u8):
+    """An 8-bit grayscale PNG of a 2-D uint8 array (filter 0 rows, zlib),
+    written here so that the decoder is timed on an independent encoding."""
+    import struct
+    import zlib
+
+    h, w = u8.shape
+    raw = b"".join(b"\x00" + u8[y].tobytes() for y in range(h))
+
+    def chunk(kind, data):
+        return struct.pack(">I", len(data)) + kind + data + struct.pack(">I", zlib.crc32(kind + data) & 0xFFFFFFFF)
+
+    return (b"\x89PNG\r\n\x1a\n" + chunk(b"IHDR", struct.pack(">IIBBBBB", w, h, 8, 0, 0, 0, 0)) +
+            chunk(b"IDAT", zlib.compress(raw, 6)) + chunk(b"IEND", b""))
 
 
 def run_config4(args, local):

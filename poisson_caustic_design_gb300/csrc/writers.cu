@@ -7,8 +7,10 @@
 // order follow it, including the second SVG loop's use of res_x as its
 // bound (utils.cpp:292).  Files are written in full or not at all: a file
 // that cannot be opened returns PCD_BAD_ARG (the reference prints to cerr).
+#include <algorithm>
 #include <cstdio>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "api_internal.cuh"
@@ -25,11 +27,52 @@ std::string g(double v)
     return buf;
 }
 
-std::string f(double v)
+// number formats appended in place (no temporaries)
+void app_g(std::string &t, double v)
+{
+    char buf[64];
+    const int k = std::snprintf(buf, sizeof(buf), "%g", v);
+    t.append(buf, (size_t)k);
+}
+
+void app_f(std::string &t, double v)
 {
     char buf[384];
-    std::snprintf(buf, sizeof(buf), "%f", v);
-    return buf;
+    const int k = std::snprintf(buf, sizeof(buf), "%f", v);
+    t.append(buf, (size_t)k);
+}
+
+void app_i(std::string &t, int v)
+{
+    char buf[16];
+    const int k = std::snprintf(buf, sizeof(buf), "%d", v);
+    t.append(buf, (size_t)k);
+}
+
+// Appends emit(i, text) for i = 0 .. count-1 to t, in order: ranges of at
+// least `grain` items formatted on up to 16 host threads into separate
+// buffers, then concatenated (the bytes do not depend on the thread count).
+template <class Emit>
+void parallel_text(std::string &t, long count, long grain, Emit emit)
+{
+    const long hw = std::max(1u, std::thread::hardware_concurrency());
+    const long T = std::max(1L, std::min({hw, 16L, count / std::max(1L, grain)}));
+    if (T == 1) {
+        for (long i = 0; i < count; i++) emit(i, t);
+        return;
+    }
+    std::vector<std::string> part((size_t)T);
+    std::vector<std::thread> th;
+    for (long k = 0; k < T; k++)
+        th.emplace_back([&, k] {
+            const long a = count * k / T, b = count * (k + 1) / T;
+            for (long i = a; i < b; i++) emit(i, part[(size_t)k]);
+        });
+    for (auto &x : th) x.join();
+    size_t total = t.size();
+    for (auto &p : part) total += p.size();
+    t.reserve(total);
+    for (auto &p : part) t += p;
 }
 
 int write_file(const char *filename, const std::string &text)
@@ -78,26 +121,43 @@ int write_solid_obj(const double *front, const double *back, int nx, int ny, dou
     t += "# Generated by the software algorithm written by Dylan Missuwe\n";
     t += "# The algorithm used to create the lens is based on the paper "
          "\"Poisson-Based Continuous Surface Generation for Goal-Based Caustics\" by Yue et al (2014)\n";
-    for (int i = 0; i < n; i++)
-        t += "v " + g(width - front[3 * i]) + " " + g(height - front[3 * i + 1]) + " " + g(-(front[3 * i + 2])) + "\n";
-    for (int i = 0; i < n; i++)
-        t += "v " + g(width - back[3 * i]) + " " + g(height - back[3 * i + 1]) + " " + g(-thickness - min_h) + "\n";
-    // structured-mesh triangles (mesh.cpp:57-63), then the same reversed for the back
-    auto face = [&](int a, int b, int c) {
-        t += "f " + std::to_string(a) + " " + std::to_string(b) + " " + std::to_string(c) + "\n";
+    auto vert = [](std::string &s, double a, double b, double c) {
+        s += "v ";
+        app_g(s, a);
+        s += ' ';
+        app_g(s, b);
+        s += ' ';
+        app_g(s, c);
+        s += '\n';
     };
-    for (int y = 0; y < ny - 1; y++)
-        for (int x = 0; x < nx - 1; x++) {
-            const int i = y * nx + x;
-            face(i + 1, i + 2, i + nx + 1);
-            face(i + nx + 1, i + 2, i + nx + 2);
-        }
-    for (int y = 0; y < ny - 1; y++)
-        for (int x = 0; x < nx - 1; x++) {
-            const int i = y * nx + x;
-            face(i + n + 1, i + nx + n + 1, i + 1 + n + 1);
-            face(i + nx + n + 1, i + nx + 1 + n + 1, i + 1 + n + 1);
-        }
+    parallel_text(t, n, 4096, [&](long i, std::string &s) {
+        vert(s, width - front[3 * i], height - front[3 * i + 1], -(front[3 * i + 2]));
+    });
+    parallel_text(t, n, 4096, [&](long i, std::string &s) {
+        vert(s, width - back[3 * i], height - back[3 * i + 1], -thickness - min_h);
+    });
+    // structured-mesh triangles (mesh.cpp:57-63), then the same reversed for the back
+    auto face_to = [](std::string &s, int a, int b, int c) {
+        s += "f ";
+        app_i(s, a);
+        s += ' ';
+        app_i(s, b);
+        s += ' ';
+        app_i(s, c);
+        s += '\n';
+    };
+    const long cells = (long)(nx - 1) * (ny - 1);
+    parallel_text(t, cells, 4096, [&](long k, std::string &s) {
+        const int y = (int)(k / (nx - 1)), x = (int)(k - (long)y * (nx - 1)), i = y * nx + x;
+        face_to(s, i + 1, i + 2, i + nx + 1);
+        face_to(s, i + nx + 1, i + 2, i + nx + 2);
+    });
+    parallel_text(t, cells, 4096, [&](long k, std::string &s) {
+        const int y = (int)(k / (nx - 1)), x = (int)(k - (long)y * (nx - 1)), i = y * nx + x;
+        face_to(s, i + n + 1, i + nx + n + 1, i + 1 + n + 1);
+        face_to(s, i + nx + n + 1, i + nx + 1 + n + 1, i + 1 + n + 1);
+    });
+    auto face = [&](int a, int b, int c) { face_to(t, a, b, c); };
     // side wall between the front and back perimeters (utils.cpp:243-256)
     const std::vector<int> per = perimeter(nx, ny);
     for (size_t k = 0; k < per.size(); ++k) {
@@ -122,26 +182,29 @@ int write_grid_svg(const double *pts, int nx, int ny, double width, double heigh
     t += "<svg width=\"1000\" height=\"" + g(1000.0f * aspect) +
          "\" xmlns=\"http://www.w3.org/2000/svg\" xmlns:xlink=\"http://www.w3.org/1999/xlink\">\n";
     t += "<rect width=\"100%\" height=\"100%\" fill=\"white\"/>\n";
-    auto coord = [&](int idx) {
-        return f((pts[3 * idx] / width) * 1000.0f) + "," + f((pts[3 * idx + 1] / height) * 1000.0f * aspect);
+    auto coord = [&](std::string &s, int idx) {
+        app_f(s, (pts[3 * idx] / width) * 1000.0f);
+        s += ',';
+        app_f(s, (pts[3 * idx + 1] / height) * 1000.0f * aspect);
     };
     const std::string tail = "\" fill=\"none\" stroke=\"black\" stroke-width=\"" + g(stroke_width) + "\"/>\n";
-    for (int j = 0; j < ny; j++) {
-        std::string path = "M";
+    // one path a row, then one a column, each formatted on its own
+    parallel_text(t, ny, 8, [&](long j, std::string &s) {
+        s += "<path d=\"M";
         for (int i = 0; i < nx; i++) {
-            path += coord(i + j * nx);
-            if (i < nx - 1) path += "L";
+            coord(s, i + (int)j * nx);
+            if (i < nx - 1) s += 'L';
         }
-        t += "<path d=\"" + path + tail;
-    }
-    for (int j = 0; j < nx; j++) {
-        std::string path = "M";
+        s += tail;
+    });
+    parallel_text(t, nx, 8, [&](long j, std::string &s) {
+        s += "<path d=\"M";
         for (int i = 0; i < ny; i++) {
-            path += coord(j + i * nx);
-            if (i < nx - 1) path += "L";  // the reference bounds this loop's separators by res_x
+            coord(s, (int)j + i * nx);
+            if (i < nx - 1) s += 'L';  // the reference bounds this loop's separators by res_x
         }
-        t += "<path d=\"" + path + tail;
-    }
+        s += tail;
+    });
     t += "</svg>\n";
     return write_file(filename, t);
 }
@@ -153,15 +216,15 @@ int write_heightmap_json(const double *h, int width, int height, const char *fil
         return PCD_BAD_ARG;
     }
     std::string t = "[\n";
-    for (int i = 0; i < height; ++i) {
-        t += "  [";
+    parallel_text(t, height, 8, [&](long i, std::string &s) {
+        s += "  [";
         for (int j = 0; j < width; ++j) {
-            t += g(h[(size_t)i * width + j]);
-            if (j < width - 1) t += ", ";
+            app_g(s, h[(size_t)i * width + j]);
+            if (j < width - 1) s += ", ";
         }
-        t += "]";
-        t += i < height - 1 ? ",\n" : "\n";
-    }
+        s += "]";
+        s += i < height - 1 ? ",\n" : "\n";
+    });
     t += "]\n";
     return write_file(filename, t);
 }
