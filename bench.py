@@ -704,7 +704,10 @@ def run_ours(args, rank, world, local, pg):
         for w in range(args.warmup):
             ctx.solve(hb[w % len(hb)].numpy(), hphi.numpy(), hopts)
         barrier(pg)
-        for k in range(args.steps):
+        # host-timed, so a single stall of the host (the clock sampler's
+        # nvidia-smi queries the driver meanwhile) moves a short mean: three
+        # samples per step, all of them averaged
+        for k in range(3 * args.steps):
             flush.zero_()
             torch.cuda.synchronize()
             t = time.perf_counter()
@@ -847,7 +850,8 @@ def run_ours(args, rank, world, local, pg):
         "roofline_stream_4096": stream_roof,
         "roofline": roof,
         "cpu_baseline": cpu,
-        "e2e": ({"value": e2e, "unit": UNIT, "h2d_bytes_per_step": cells * 8, "d2h_bytes_per_step": cells * 8}
+        "e2e": ({"value": e2e, "unit": UNIT, "h2d_bytes_per_step": cells * 8, "d2h_bytes_per_step": cells * 8,
+                 "samples": len(e2e_ms), "median": float(np.median(e2e_ms))}
                 if e2e is not None else None),
         "gpu_launches": int(launches),
         "gpu_launches_per_step": int(launches) / args.steps,
